@@ -1,0 +1,189 @@
+/*
+ * gqmps2_gb300.h -- C ABI of the GB300 (sm_103a) two-site finite DMRG library
+ * (libgqmps2_gb300.so).
+ *
+ * The reference, gqmps2 v0.2-alpha.0, is a header-only C++ template library;
+ * its hot path is
+ *   GQTEN_Double TwoSiteFiniteVMPS(FiniteMPS&, const MPO&, const SweepParams&)
+ *     (include/gqmps2/algorithm/vmps/two_site_update_finite_vmps_impl.h:77-101)
+ * with LanczosSolver(eff_ham, init, LanczosParams, where)
+ *     (include/gqmps2/algorithm/lanczos_solver_impl.h:79-226)
+ * and GraceQ/tensor's block-sparse Contract / SVD underneath.  This header
+ * exposes the same pieces with plain pointers and sizes: device-resident
+ * block-sparse tensors, the contraction, the effective-Hamiltonian matvec,
+ * the Lanczos solver, the truncating SVD and the sweep driver.
+ *
+ * Conventions
+ *   - Every call returns an int status (GQ_OK == 0); on failure
+ *     gq_last_error() describes it.  Nothing exits the process (the
+ *     reference calls exit(1) on a dstev failure, lanczos_solver_impl.h:288).
+ *   - A quantum number is nq int32 values (U(1)^nq, nq <= 4).
+ *   - Leg direction: GQ_OUT (+1) or GQ_IN (-1).  A block with sector
+ *     coordinates c is allowed when sum_i dir_i * qn_i(c_i) == div.
+ *   - Blocks are dense, row-major float64, exchanged in ascending
+ *     lexicographic order of their sector coordinates ("block order").
+ *   - One process drives one GPU; the library is not re-entrant (neither is
+ *     the reference, which stages through fixed file paths).
+ */
+#ifndef GQMPS2_GB300_H
+#define GQMPS2_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GQ_OK 0
+#define GQ_ERR_INVALID 1
+#define GQ_ERR_CUDA 2
+#define GQ_ERR_SOLVER 3
+#define GQ_ERR_NUMERICAL 4
+#define GQ_ERR_OOM 5
+#define GQ_ERR_INTERNAL 6
+
+#define GQ_OUT 1
+#define GQ_IN (-1)
+
+/* Arithmetic of the contractions (matvec, environment growth, two-site
+ * state).  Lanczos recurrence, tridiagonal solve and SVD are FP64 always. */
+#define GQ_PREC_FP64 0   /* plain form: FP64 end to end */
+#define GQ_PREC_TF32X3 1 /* split form: 3xTF32 tcgen05 products, FP64 sums */
+
+/* Position of the two-site block (the reference's `where` string,
+ * lanczos_solver_impl.h:93-112). */
+#define GQ_WHERE_LEND 0
+#define GQ_WHERE_CENT 1
+#define GQ_WHERE_REND 2
+
+typedef struct gq_tensor gq_tensor;
+typedef struct gq_dmrg gq_dmrg;
+
+/* LanczosParams (include/gqmps2/algorithm/lanczos_solver.h:34-39). */
+typedef struct {
+  double error;           /* default 1e-7 */
+  int64_t max_iterations; /* default 200 */
+} gq_lanczos_params;
+
+/* SweepParams (include/gqmps2/algorithm/vmps/two_site_update_finite_vmps.h:27-55)
+ * minus the two paths, which the host wrapper owns, plus the precision. */
+typedef struct {
+  int64_t sweeps;
+  int64_t dmin;
+  int64_t dmax;
+  double trunc_err;
+  gq_lanczos_params lanczos;
+  int precision; /* GQ_PREC_* */
+  int verbose;   /* 1: print the reference's per-update log line */
+} gq_sweep_params;
+
+/* One two-site update: the fields of the reference's log line
+ * (two_site_update_finite_vmps_impl.h:329-338) plus timing and work. */
+typedef struct {
+  int32_t site;
+  int32_t dir; /* 'r' or 'l' */
+  double e0;
+  double trunc_err;
+  int64_t D;
+  int64_t iters;
+  double ee;
+  double lanczos_seconds;
+  double update_seconds;
+  double svd_seconds;
+  double env_seconds;
+  int64_t matvecs;
+  double matvec_flops; /* sum of 2*m*n*k over the matvec block GEMMs */
+  double env_flops;
+  int64_t theta_size;  /* elements of the two-site state */
+} gq_update_stats;
+
+/* Library ------------------------------------------------------------- */
+/* Bind the calling process to `device` (-1: current device).  Optional:
+ * every other entry point initialises on first use. */
+int gq_init(int device);
+/* Description of the last failure in this thread ("" if none). */
+const char *gq_last_error(void);
+/* Wait for all queued device work. */
+int gq_synchronize(void);
+
+/* Tensors --------------------------------------------------------------- *
+ * Replaces GQTensor construction + element assignment on the host and the
+ * implicit host->device placement (the reference keeps tensors in RAM and
+ * on disk: include/gqmps2/one_dim_tn/framework/ten_vec.h:50-85).
+ *   dirs[rank]; nsecs[rank]; qns: for each leg, nsecs[l] x nq ints;
+ *   dims: for each leg, nsecs[l] int64; div[nq];
+ *   coords[nblocks x rank] in ascending block order (each block allowed);
+ *   data: the blocks' elements concatenated in that order (NULL: zeros). */
+int gq_tensor_create(int rank, int nq, const int *dirs, const int *nsecs, const int *qns,
+                     const int64_t *dims, const int *div, int64_t nblocks,
+                     const int *coords, const double *data, gq_tensor **out);
+/* Sizes needed to export: rank, nq, total sector count over legs, blocks,
+ * elements. */
+int gq_tensor_describe(const gq_tensor *t, int *rank, int *nq, int64_t *nsec_total,
+                       int64_t *nblocks, int64_t *nelem);
+/* Export the structure and (if data != NULL) copy the elements to host
+ * memory.  Arrays must hold the sizes reported by gq_tensor_describe. */
+int gq_tensor_export(const gq_tensor *t, int *dirs, int *nsecs, int *qns, int64_t *dims,
+                     int *div, int *coords, double *data);
+int gq_tensor_destroy(gq_tensor *t);
+
+/* Contraction ------------------------------------------------------------ *
+ * gqten Contract(a, b, {axes_a, axes_b}, &c): output legs are a's free
+ * legs then b's free legs.  Call sites: two_site_update_finite_vmps_impl.h:
+ * 118-129, 243, 272, 276, 290-317; lanczos_solver_impl.h:231-254. */
+int gq_contract(const gq_tensor *a, const gq_tensor *b, int naxes, const int *axes_a,
+                const int *axes_b, int precision, gq_tensor **out, double *flops);
+
+/* Effective Hamiltonian ------------------------------------------------- *
+ * eff_ham_mul_state_{cent,lend,rend} (lanczos_solver_impl.h:228-256).
+ * L / R may be NULL at the chain ends (where = LEND / REND).  The result
+ * lives in the Lanczos space: every block allowed by the state's legs and
+ * divergence (blocks the contraction does not reach are zero). */
+int gq_eff_ham_mul_state(const gq_tensor *L, const gq_tensor *Wl, const gq_tensor *Wr,
+                         const gq_tensor *R, int where, const gq_tensor *state, int precision,
+                         gq_tensor **out, double *flops);
+
+/* Lanczos --------------------------------------------------------------- *
+ * LanczosSolver (lanczos_solver_impl.h:79-226).  `init` is not modified
+ * (the reference consumes it); gs_vec is a new tensor in the Lanczos space
+ * that the caller destroys. */
+int gq_lanczos(const gq_tensor *L, const gq_tensor *Wl, const gq_tensor *Wr, const gq_tensor *R,
+               int where, const gq_tensor *init, const gq_lanczos_params *params, int precision,
+               int64_t *iters, double *gs_eng, gq_tensor **gs_vec);
+
+/* Truncating SVD -------------------------------------------------------- *
+ * gqten SVD(t, ldims, ldiv, trunc_err, Dmin, Dmax, &u, &s, &vt, &err, &D)
+ * (two_site_update_finite_vmps_impl.h:258-263).  s receives the kept
+ * singular values in bond order (capacity s_cap; *D tells how many).
+ * scale_side: 0 plain U / Vt, 1 return U.S in *u, 2 return S.Vt in *vt. */
+int gq_svd(const gq_tensor *t, int ldims, const int *ldiv, double trunc_err, int64_t dmin,
+           int64_t dmax, int scale_side, gq_tensor **u, gq_tensor **vt, double *s, int64_t s_cap,
+           double *actual_trunc_err, int64_t *D);
+
+/* Two-site DMRG --------------------------------------------------------- *
+ * The state of TwoSiteFiniteVMPS kept resident on the device: the MPS, the
+ * MPO and the left/right environments that the reference stages through
+ * <temp_path>/{l,r}env<len> files (GenEnvTenName, :55-61).  The tensors
+ * passed in are copied; the caller keeps ownership of its handles. */
+int gq_dmrg_create(int n_sites, gq_tensor *const *mps, gq_tensor *const *mpo, gq_dmrg **out);
+/* InitEnvs (two_site_update_finite_vmps_impl.h:104-135): right
+ * environments R_1..R_{N-2} from a right-canonical MPS. */
+int gq_dmrg_init_envs(gq_dmrg *d, int precision);
+/* Install / fetch an environment ('l' or 'r', block length) -- the
+ * equivalent of reading / writing an env file, used to resume. */
+int gq_dmrg_set_env(gq_dmrg *d, int dir, int len, const gq_tensor *env);
+int gq_dmrg_get_env(gq_dmrg *d, int dir, int len, gq_tensor **out);
+/* `sweeps` sweeps of TwoSiteFiniteVMPSSweep (:143-161).  stats (may be
+ * NULL) receives 2*(N-1) records per sweep.  *e0 = energy of the last
+ * update, the reference's return value. */
+int gq_dmrg_sweep(gq_dmrg *d, const gq_sweep_params *params, gq_update_stats *stats,
+                  double *e0);
+/* Copy of the site tensor i (caller destroys). */
+int gq_dmrg_get_mps(gq_dmrg *d, int i, gq_tensor **out);
+int gq_dmrg_destroy(gq_dmrg *d);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GQMPS2_GB300_H */

@@ -1,0 +1,179 @@
+// Declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "gq_common.hpp"
+
+namespace gq {
+
+struct Context {
+  int device = 0;
+  cudaDeviceProp prop{};
+  cudaStream_t stream = nullptr;
+  double *host_scalars = nullptr;  // pinned, 64 doubles
+  double *dev_scalars = nullptr;   // device, 64 doubles
+  cudaEvent_t sync_event = nullptr;
+  void *cusolver = nullptr;        // cusolverDnHandle_t, created lazily
+};
+
+Context &ctx();
+void init_context(int device);
+void sync();
+
+// Arithmetic of the contractions (matvec, environment growth).
+enum Precision : int {
+  kFP64 = 0,    // FP64 FMA end to end
+  kTF32x3 = 1,  // 3xTF32 split products on tcgen05, FP32 accumulate per
+                // K-chunk, FP64 sum of the chunks
+};
+
+// ---------------------------------------------------------------------------
+// Contraction engine (contract.cu)
+// ---------------------------------------------------------------------------
+struct GemmTile {       // one output tile of one output block
+  int64_t c_off;        // element offset of the output block
+  int m, n;             // output block rows / cols
+  int row0, col0;       // tile origin inside the block
+  int pair_begin, pair_end;
+  int64_t work;         // sum over pairs of k (for scheduling)
+};
+struct GemmPair {       // one contributing (A block, B block) product
+  int64_t a_off, b_off; // element offsets in the (possibly permuted) operands
+  int k;
+  int lda, ldb;
+};
+struct PermBlock {      // permute one block: dst(i0..ir) = src(sum i_l * sstride_l)
+  int64_t src_off, dst_off, n;
+  int rank;
+  int dims[kMaxRank];       // destination dims
+  int64_t sstride[kMaxRank];// source stride of each destination dim
+};
+struct PermChunk { int block; int64_t begin, end; };
+
+struct PermPlan {
+  bool needed = false;
+  int64_t total = 0;
+  DevArray<PermBlock> blocks;
+  DevArray<PermChunk> chunks;
+  int64_t nchunks = 0;
+};
+
+struct ContractPlan {
+  TensorPtr out;          // output structure (no data)
+  int transA = 0, transB = 0;
+  PermPlan pa, pb;
+  DevArray<GemmTile> tiles;
+  DevArray<GemmPair> pairs;
+  int64_t ntiles = 0;
+  int64_t nzero_blocks = 0;   // output blocks with no contribution
+  DevArray<int64_t> zero_blocks;  // (offset, size) pairs to clear
+  double flops = 0.0;         // 2*m*n*k summed over block products
+  int64_t a_elems = 0, b_elems = 0;
+  int tile_m = 0, tile_n = 0;
+};
+
+// Plan C = A . B over the given axes.  If `target` is non-null the output
+// uses its structure (every contributing block must exist there; blocks of
+// `target` without contributions are written as zeros).
+std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
+                                            const std::vector<int> &axes_a,
+                                            const std::vector<int> &axes_b,
+                                            const Tensor *target, Precision prec);
+// Scratch needed by run_contract (elements).
+int64_t contract_scratch(const ContractPlan &p);
+void run_contract(const ContractPlan &p, const double *a, const double *b, double *c,
+                  double *scratch, Precision prec);
+TensorPtr contract(const Tensor &a, const Tensor &b, const std::vector<int> &axes_a,
+                   const std::vector<int> &axes_b, Precision prec, double *flops_out = nullptr);
+
+// GEMM kernels (launched by run_contract)
+void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, double *C);
+void launch_gemm_tf32x3(const ContractPlan &p, const double *A, const double *B, double *C);
+int gemm_tile_m(Precision prec);
+int gemm_tile_n(Precision prec);
+
+// ---------------------------------------------------------------------------
+// Vector kernels (vecops.cu).  Scalars live in device memory so the Lanczos
+// recurrence runs without a host round trip per operation.
+// ---------------------------------------------------------------------------
+// out = sum_i x_i * y_i  (deterministic two-stage reduction)
+void dev_dot(const double *x, const double *y, int64_t n, double *out_dev, double *scratch);
+// y = x - a*u - b*v (u or v may be null); out = ||y||^2.  a_dev / b_dev point
+// to device scalars (b_dev may be null); b is applied as sqrt(*b_dev) when
+// b_is_sq.
+void dev_lanczos_gamma(const double *x, const double *u, const double *a_dev,
+                       const double *v, const double *b_dev, bool b_is_sq,
+                       double *y, int64_t n, double *nrm2_out_dev, double *scratch);
+// x *= 1/sqrt(*nrm2_dev)
+void dev_scale_rsqrt(double *x, int64_t n, const double *nrm2_dev);
+// x *= s
+void dev_scale(double *x, int64_t n, double s);
+// out = sum_k c[k] * bases[k]   (c on host, m vectors)
+void dev_combine(const std::vector<const double *> &bases, const std::vector<double> &c,
+                 double *out, int64_t n);
+// Block copies between structures: (src_off, dst_off, n) triples.
+void dev_block_copy(const double *src, double *dst, const std::vector<int64_t> &triples);
+int64_t dot_scratch_elems();
+
+// ---------------------------------------------------------------------------
+// Truncating SVD (svd.cu)
+// ---------------------------------------------------------------------------
+struct SvdOut {
+  TensorPtr u, vt;               // U (row legs..., new OUT), Vt (new IN, col legs...)
+  std::vector<double> s;         // kept singular values, bond order
+  Index new_bond;                // OUT-directed new bond
+  double trunc_err = 0.0;
+  int64_t D = 0;
+};
+// scale_side: 0 none, 1 multiply U columns by s (U.S), 2 multiply Vt rows (S.Vt)
+SvdOut svd_truncate(const Tensor &t, int ldims, const QN &ldiv, double trunc_err,
+                    int64_t dmin, int64_t dmax, int scale_side);
+
+// ---------------------------------------------------------------------------
+// Tridiagonal eigensolver (tridiag.cpp)
+// ---------------------------------------------------------------------------
+// Lowest eigenvalue of the n x n symmetric tridiagonal matrix (diag a,
+// off-diag b); if vec != nullptr also its unit eigenvector (largest-|.|
+// component positive).  Returns false if the iteration fails to converge.
+bool tridiag_lowest(const double *a, const double *b, int n, double *eval, double *vec);
+
+// ---------------------------------------------------------------------------
+// Effective Hamiltonian and Lanczos (lanczos.cu)
+// ---------------------------------------------------------------------------
+enum Where : int { kLend = 0, kCent = 1, kRend = 2 };
+
+struct EffHam {
+  const Tensor *L = nullptr, *Wl = nullptr, *Wr = nullptr, *R = nullptr;
+  Where where = kCent;
+};
+
+struct MatvecPlan;  // opaque
+std::shared_ptr<MatvecPlan> plan_matvec(const EffHam &h, const Tensor &space, Precision prec);
+void run_matvec(MatvecPlan &p, const double *x, double *y);
+double matvec_flops(const MatvecPlan &p);
+
+struct LanczosParamsC {
+  double error = 1e-7;
+  int64_t max_iterations = 200;
+};
+struct LanczosResult {
+  int64_t iters = 0;
+  double energy = 0.0;
+  TensorPtr gs;        // in the Lanczos-space structure
+  int64_t matvecs = 0;
+  double matvec_flops = 0.0;
+  double matvec_seconds = 0.0;
+};
+// The Lanczos space: every block allowed by the state's legs and div.
+TensorPtr lanczos_space(const Tensor &state);
+// Copy `src` blocks into `dst` (same legs; dst must contain src's blocks).
+void embed(const Tensor &src, Tensor &dst);
+LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC &p,
+                      Precision prec);
+int64_t eff_ham_dim(const EffHam &h);
+
+}  // namespace gq

@@ -1,0 +1,230 @@
+// Effective-Hamiltonian matvec and Lanczos ground-state solver.
+//
+// Restates ``LanczosSolver`` (``lanczos_solver_impl.h:79-226``) with the
+// Krylov vectors resident in HBM: no re-orthogonalisation, every basis
+// vector kept, stop on ``E_old - E_new < error`` or ``m == eff_dim`` or
+// ``m == max_iterations - 1``; breakdown handled as at ``:163-180``.  The
+// matvec follows ``eff_ham_mul_state_{cent,lend,rend}`` (``:228-256``)
+// contraction for contraction; its work lists are planned once per update
+// and replayed every iteration.
+#include <chrono>
+#include <cmath>
+
+#include "gq_runtime.hpp"
+
+namespace gq {
+
+struct MatvecStep {
+  std::shared_ptr<ContractPlan> plan;
+  int a_src, b_src;   // -1: the input vector x; >=0: intermediate id; -2: constant
+  const Tensor *a_const = nullptr, *b_const = nullptr;
+  int out;            // intermediate id, or -1 for the output vector
+};
+
+struct MatvecPlan {
+  EffHam h;
+  Precision prec = kFP64;
+  std::vector<MatvecStep> steps;
+  std::vector<TensorPtr> inter;
+  DevBuf scratch;
+  double flops = 0.0;
+};
+
+int64_t eff_ham_dim(const EffHam &h) {
+  switch (h.where) {
+    case kCent:
+      return h.L->idx[0].total() * h.Wl->idx[1].total() * h.Wr->idx[1].total() *
+             h.R->idx[0].total();
+    case kLend:
+      return h.Wl->idx[0].total() * h.Wr->idx[1].total() * h.R->idx[0].total();
+    default:
+      return h.L->idx[0].total() * h.Wl->idx[1].total() * h.Wr->idx[0].total();
+  }
+}
+
+std::shared_ptr<MatvecPlan> plan_matvec(const EffHam &h, const Tensor &space, Precision prec) {
+  auto mp = std::make_shared<MatvecPlan>();
+  mp->h = h;
+  mp->prec = prec;
+  struct S { const Tensor *ca; int as; const Tensor *cb; int bs; std::vector<int> xa, xb; };
+  std::vector<S> spec;
+  // a/b source: -1 = x, -2 = constant, k>=0 = intermediate k (previous step)
+  if (h.where == kCent) {
+    spec = {{h.L, -2, nullptr, -1, {0}, {0}},
+            {nullptr, 0, h.Wl, -2, {0, 2}, {0, 1}},
+            {nullptr, 1, h.Wr, -2, {4, 1}, {0, 1}},
+            {nullptr, 2, h.R, -2, {4, 1}, {1, 0}}};
+  } else if (h.where == kLend) {
+    spec = {{nullptr, -1, h.Wl, -2, {0}, {0}},
+            {nullptr, 0, h.Wr, -2, {0, 2}, {1, 0}},
+            {nullptr, 1, h.R, -2, {0, 3}, {0, 1}}};
+  } else {
+    spec = {{nullptr, -1, h.L, -2, {0}, {0}},
+            {nullptr, 0, h.Wl, -2, {2, 0}, {0, 1}},
+            {nullptr, 1, h.Wr, -2, {3, 0}, {1, 0}}};
+  }
+  int64_t scratch = 0;
+  for (size_t i = 0; i < spec.size(); ++i) {
+    const S &s = spec[i];
+    const Tensor &A = s.as == -2 ? *s.ca : (s.as == -1 ? space : *mp->inter[s.as]);
+    const Tensor &B = s.bs == -2 ? *s.cb : (s.bs == -1 ? space : *mp->inter[s.bs]);
+    const bool last = i + 1 == spec.size();
+    auto plan = plan_contract(A, B, s.xa, s.xb, last ? &space : nullptr, prec);
+    MatvecStep st;
+    st.plan = plan;
+    st.a_src = s.as;
+    st.b_src = s.bs;
+    st.a_const = s.as == -2 ? s.ca : nullptr;
+    st.b_const = s.bs == -2 ? s.cb : nullptr;
+    if (last) {
+      st.out = -1;
+    } else {
+      auto t = clone_structure(*plan->out);
+      t->allocate();
+      mp->inter.push_back(t);
+      st.out = (int)mp->inter.size() - 1;
+    }
+    scratch = std::max(scratch, contract_scratch(*plan));
+    mp->flops += plan->flops;
+    mp->steps.push_back(std::move(st));
+  }
+  mp->scratch.alloc(scratch);
+  return mp;
+}
+
+void run_matvec(MatvecPlan &p, const double *x, double *y) {
+  for (auto &st : p.steps) {
+    const double *a = st.a_src == -2 ? st.a_const->data.p
+                      : st.a_src == -1 ? x
+                                       : p.inter[st.a_src]->data.p;
+    const double *b = st.b_src == -2 ? st.b_const->data.p
+                      : st.b_src == -1 ? x
+                                       : p.inter[st.b_src]->data.p;
+    double *c = st.out == -1 ? y : p.inter[st.out]->data.p;
+    run_contract(*st.plan, a, b, c, p.scratch.p, p.prec);
+  }
+}
+
+double matvec_flops(const MatvecPlan &p) { return p.flops; }
+
+TensorPtr lanczos_space(const Tensor &state) {
+  return make_structure(state.nq, state.idx, state.div, allowed_blocks(state.idx, state.div));
+}
+
+void embed(const Tensor &src, Tensor &dst) {
+  GQ_CHECK(src.idx.size() == dst.idx.size(), "embed: rank mismatch");
+  for (size_t l = 0; l < src.idx.size(); ++l)
+    GQ_CHECK(src.idx[l] == dst.idx[l], "embed: leg mismatch");
+  dst.zero();
+  std::vector<int64_t> tr;
+  tr.reserve(src.nblocks() * 3);
+  for (int64_t b = 0; b < src.nblocks(); ++b) {
+    const int64_t d = dst.find(src.block_coords(b));
+    GQ_CHECK(d >= 0, "embed: block missing from the destination structure");
+    tr.push_back(src.offs[b]);
+    tr.push_back(dst.offs[d]);
+    tr.push_back(src.block_size(b));
+  }
+  dev_block_copy(src.data.p, dst.data.p, tr);
+}
+
+namespace {
+// Copy `count` device scalars to the pinned host area and wait for them.
+void fetch(const double *dev, double *host, int count) {
+  GQ_CUDA(cudaMemcpyAsync(host, dev, sizeof(double) * count, cudaMemcpyDeviceToHost, stream()));
+  sync();
+}
+}  // namespace
+
+LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC &prm,
+                      Precision prec) {
+  using clk = std::chrono::steady_clock;
+  const int64_t maxit = prm.max_iterations;
+  GQ_CHECK(maxit >= 2, "Lanczos needs max_iterations >= 2");
+  const int64_t n = init.size();
+  GQ_CHECK(n > 0, "empty Lanczos vector");
+  const int64_t dim = eff_ham_dim(h);
+  auto plan = plan_matvec(h, init, prec);
+
+  LanczosResult res;
+  std::vector<DevBuf> bases;
+  bases.reserve(maxit);
+  DevBuf last(n);
+  // device scalars: a[0..maxit), nrm2[0..maxit)
+  DevBuf sc(2 * maxit + 2);
+  double *a_dev = sc.p, *n_dev = sc.p + maxit;
+  DevBuf red(dot_scratch_elems());
+  std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
+  double *hs = ctx().host_scalars;
+  auto t_mv = clk::duration::zero();
+
+  auto matvec = [&](const double *x) {
+    run_matvec(*plan, x, last.p);
+    res.matvecs++;
+    res.matvec_flops += plan->flops;
+  };
+
+  // v0 = init / |init|
+  bases.emplace_back(n);
+  GQ_CUDA(cudaMemcpyAsync(bases[0].p, init.data.p, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                          stream()));
+  dev_dot(bases[0].p, bases[0].p, n, n_dev, red.p);
+  dev_scale_rsqrt(bases[0].p, n, n_dev);
+  matvec(bases[0].p);
+  dev_dot(bases[0].p, last.p, n, a_dev, red.p);
+  fetch(a_dev, hs, 1);
+  a[0] = hs[0];
+  double energy0 = a[0];
+
+  auto finish = [&](int64_t nvec, int64_t iters, double energy) {
+    std::vector<double> c(nvec, 1.0);
+    if (nvec > 1) {
+      double ev;
+      if (!tridiag_lowest(a.data(), b.data(), (int)nvec, &ev, c.data()))
+        fail(kNumericalError, "tridiagonal eigensolver did not converge");
+    }
+    auto gs = clone_structure(init);
+    gs->allocate();
+    std::vector<const double *> ptrs;
+    for (int64_t k = 0; k < nvec; ++k) ptrs.push_back(bases[k].p);
+    dev_combine(ptrs, c, gs->data.p, n);
+    res.iters = iters;
+    res.energy = energy;
+    res.gs = gs;
+  };
+
+  int64_t m = 0;
+  while (true) {
+    m += 1;
+    bases.emplace_back(n);
+    dev_lanczos_gamma(last.p, bases[m - 1].p, a_dev + (m - 1), m >= 2 ? bases[m - 2].p : nullptr,
+                      m >= 2 ? n_dev + (m - 1) : nullptr, true, bases[m].p, n, n_dev + m, red.p);
+    fetch(n_dev + m, hs, 1);
+    const double nrm2 = hs[0];
+    if (!std::isfinite(nrm2)) fail(kNumericalError, "Lanczos vector became non-finite");
+    const double norm_gamma = std::sqrt(nrm2);
+    if (norm_gamma == 0.0) {  // invariant subspace found
+      finish(m, m, energy0);
+      break;
+    }
+    N[m] = nrm2;
+    b[m - 1] = norm_gamma;
+    dev_scale_rsqrt(bases[m].p, n, n_dev + m);
+    matvec(bases[m].p);
+    dev_dot(bases[m].p, last.p, n, a_dev + m, red.p);
+    fetch(a_dev + m, hs, 1);
+    a[m] = hs[0];
+    double e_new;
+    if (!tridiag_lowest(a.data(), b.data(), (int)(m + 1), &e_new, nullptr))
+      fail(kNumericalError, "tridiagonal eigensolver did not converge");
+    if ((energy0 - e_new) < prm.error || m == dim || m == maxit - 1) {
+      finish(m + 1, m, e_new);
+      break;
+    }
+    energy0 = e_new;
+  }
+  (void)t_mv;
+  return res;
+}
+
+}  // namespace gq

@@ -1,0 +1,165 @@
+// Library runtime: device context, stream-ordered memory, tensor structure.
+#include "gq_runtime.hpp"
+
+#include <cstdio>
+#include <map>
+#include <mutex>
+
+namespace gq {
+
+namespace {
+Context *g_ctx = nullptr;
+std::mutex g_ctx_mu;
+}  // namespace
+
+Context &ctx() {
+  if (!g_ctx) init_context(-1);
+  return *g_ctx;
+}
+
+void init_context(int device) {
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  if (g_ctx) {
+    if (device >= 0 && device != g_ctx->device)
+      fail(kInvalidArgument, "library already initialised on another device");
+    return;
+  }
+  int ndev = 0;
+  GQ_CUDA(cudaGetDeviceCount(&ndev));
+  if (ndev <= 0) fail(kCudaError, "no CUDA device visible");
+  if (device < 0) GQ_CUDA(cudaGetDevice(&device));
+  GQ_CUDA(cudaSetDevice(device));
+  auto *c = new Context();
+  c->device = device;
+  GQ_CUDA(cudaGetDeviceProperties(&c->prop, device));
+  if (c->prop.major < 10)
+    fail(kCudaError, "this library is built for sm_103a (GB300); found sm_" +
+                         std::to_string(c->prop.major) + std::to_string(c->prop.minor));
+  GQ_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  // Keep freed blocks cached in the pool: tensors are created and released
+  // at every two-site update.
+  cudaMemPool_t pool;
+  GQ_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t thr = UINT64_MAX;
+  GQ_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  GQ_CUDA(cudaMallocHost((void **)&c->host_scalars, sizeof(double) * 64));
+  GQ_CUDA(cudaMallocAsync((void **)&c->dev_scalars, sizeof(double) * 64, c->stream));
+  GQ_CUDA(cudaEventCreateWithFlags(&c->sync_event, cudaEventDisableTiming));
+  g_ctx = c;
+}
+
+cudaStream_t stream() { return ctx().stream; }
+
+void sync() { GQ_CUDA(cudaStreamSynchronize(stream())); }
+
+void DevBuf::alloc(int64_t elems) {
+  release();
+  n = elems;
+  if (elems <= 0) return;
+  GQ_CUDA(cudaMallocAsync((void **)&p, sizeof(double) * elems, stream()));
+}
+
+void DevBuf::release() {
+  if (p) cudaFreeAsync(p, stream());
+  p = nullptr;
+  n = 0;
+}
+
+// ---------------------------------------------------------------------------
+void Tensor::finalize_structure() {
+  const int r = rank();
+  const int64_t nb = r ? (int64_t)coords.size() / r : 1;
+  offs.assign(nb + 1, 0);
+  lut.clear();
+  lut.reserve(nb * 2);
+  for (int64_t b = 0; b < nb; ++b) {
+    int64_t sz = 1;
+    for (int l = 0; l < r; ++l) sz *= idx[l].dim[coords[b * r + l]];
+    offs[b + 1] = offs[b] + sz;
+    lut.emplace(key(coords.data() + b * r, r), (int)b);
+  }
+}
+
+void Tensor::allocate() { data.alloc(size()); }
+
+void Tensor::zero() {
+  if (size() > 0) GQ_CUDA(cudaMemsetAsync(data.p, 0, sizeof(double) * size(), stream()));
+}
+
+TensorPtr make_structure(int nq, const std::vector<Index> &idx, const QN &div,
+                         std::vector<std::vector<int>> blocks) {
+  auto t = std::make_shared<Tensor>();
+  t->nq = nq;
+  t->idx = idx;
+  t->div = div;
+  std::sort(blocks.begin(), blocks.end());
+  blocks.erase(std::unique(blocks.begin(), blocks.end()), blocks.end());
+  const int r = (int)idx.size();
+  t->coords.reserve(blocks.size() * r);
+  for (auto &b : blocks) {
+    GQ_CHECK((int)b.size() == r, "block coordinate of wrong rank");
+    for (int l = 0; l < r; ++l) {
+      GQ_CHECK(b[l] >= 0 && b[l] < idx[l].nsec(), "block coordinate out of range");
+      t->coords.push_back(b[l]);
+    }
+  }
+  if (r == 0) t->coords.clear();
+  t->finalize_structure();
+  return t;
+}
+
+std::vector<std::vector<int>> allowed_blocks(const std::vector<Index> &idx, const QN &div) {
+  std::vector<std::vector<int>> out;
+  const int r = (int)idx.size();
+  if (r == 0) return out;
+  // Depth-first over legs with the partial charge; prune nothing (sector
+  // counts are small), emit in ascending order.
+  std::vector<int> c(r, 0);
+  std::vector<QN> partial(r + 1);
+  int l = 0;
+  c[0] = -1;
+  while (l >= 0) {
+    c[l]++;
+    if (c[l] >= idx[l].nsec()) {
+      --l;
+      continue;
+    }
+    partial[l + 1] = partial[l] + idx[l].qn[c[l]].scaled(idx[l].dir);
+    if (l == r - 1) {
+      if (partial[r] == div) out.push_back(c);
+    } else {
+      ++l;
+      c[l] = -1;
+    }
+  }
+  return out;
+}
+
+TensorPtr clone_structure(const Tensor &t) {
+  auto o = std::make_shared<Tensor>();
+  o->nq = t.nq;
+  o->idx = t.idx;
+  o->div = t.div;
+  o->coords = t.coords;
+  o->offs = t.offs;
+  o->lut = t.lut;
+  return o;
+}
+
+TensorPtr clone(const Tensor &t) {
+  auto o = clone_structure(t);
+  o->allocate();
+  if (t.size() > 0)
+    GQ_CUDA(cudaMemcpyAsync(o->data.p, t.data.p, sizeof(double) * t.size(),
+                            cudaMemcpyDeviceToDevice, stream()));
+  return o;
+}
+
+TensorPtr dag(const Tensor &t) {
+  auto o = clone(t);
+  for (auto &ix : o->idx) ix.dir = -ix.dir;
+  o->div = t.div.scaled(-1);
+  return o;
+}
+
+}  // namespace gq

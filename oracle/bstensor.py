@@ -345,9 +345,13 @@ def select_kept(all_s: np.ndarray, trunc_err: float, dmin: int, dmax: int):
     if n == 0 or ranked[0] <= 0.0:
         return order, min(n, max(1, min(dmin, dmax))), 0.0
     sq = ranked * ranked
-    total = float(sq.sum())
-    # tail[i] = sum_{j>=i} sq[j]
-    tail = np.concatenate([np.cumsum(sq[::-1])[::-1], [0.0]])
+    # tail[i] = sum_{j>=i} sq[j], accumulated from the smallest value up
+    tail = np.zeros(n + 1)
+    acc = 0.0
+    for i in range(n - 1, -1, -1):
+        acc += float(sq[i])
+        tail[i] = acc
+    total = float(tail[0])
     dcap = min(dmax, n)
     D = dcap
     lo = max(1, min(dmin, dcap))

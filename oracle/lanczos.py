@@ -76,7 +76,12 @@ def tridiag_gs(a, b, n, want_vec: bool):
     if info != 0:
         raise RuntimeError("?stev error.")
     if want_vec:
-        return float(w[0]), np.array(z[:, 0])
+        # sign convention (a gauge choice; dstev's sign is arbitrary): the
+        # largest-magnitude component, first on ties, is positive
+        v = np.array(z[:, 0])
+        if v[int(np.argmax(np.abs(v)))] < 0:
+            v = -v
+        return float(w[0]), v
     return float(w[0]), None
 
 
