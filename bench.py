@@ -1,0 +1,430 @@
+#!/usr/bin/env python
+"""Benchmark: two-site finite DMRG sweep on one GB300.
+
+Workload (the configuration the headline metric is quoted on): spin-1/2
+Heisenberg open chain, L=100, J=1, U(1) Sz, total Sz=0, Neel product state
+with a seed-0 shuffled site order; the bond dimension grows
+500 -> 800 -> 1100 -> 1400 -> 1700 -> 2000 (one sweep each), Lanczos tolerance
+1e-10.  The growth sweeps up to 1700 prepare the state (untimed); then
+``--warmup`` sweeps and ``--steps`` timed sweeps run at D=2000.
+
+* ``value``: seconds per sweep at D=2000, device-resident state, CUDA events
+  on the library's stream around the timed sweeps (lower is better).  The
+  state (several GB) is far larger than L2, so no flush is needed.
+* ``e2e``: the same sweep through the C ABI from host buffers: upload of the
+  MPS, MPO and right environments, the sweep, download of the MPS and right
+  environments -- the drop-in call's work.
+* ``roofline``: the dominant kernel (the grouped block GEMM of the matvec and
+  environment growth), algorithmic flops (2*m*n*k over the QN-allowed block
+  products) / its CUDA-event time over the timed region.
+* ``cpu_baseline``: the FP64 CPU restatement (numpy + the host BLAS) on one
+  central two-site update of the same state, scaled to a sweep by the GPU's
+  own ratio of sweep time to that update's time.
+* ``--impl reference``: the same CPU restatement on the same kind of central
+  update (block structure recorded from a GPU run), the reference's own
+  gqten+MKL path being unbuildable here.
+
+Multi-GPU: a sweep is a sequential chain of updates, so N>1 runs N
+independent replicas (one per rank); value is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SCHEDULE = [500, 800, 1100, 1400, 1700, 2000]
+L_SITES = 100
+LANCZOS = (1e-10, 100)
+WORKLOAD = "heisenberg_obc_L100_Sz0_D500to2000"
+STRUCTURE_FIXTURE = os.path.join(ROOT, "tests", "golden", "bench_center_bond.json")
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", choices=["fp64", "tf32x3"], default="fp64")
+    p.add_argument("--schedule", default=",".join(map(str, SCHEDULE)),
+                   help="comma-separated D per growth sweep; the last is the timed D")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--record-structure", action="store_true",
+                   help="write the central-bond block structure fixture")
+    return p.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def _fp64_peak_tflops(torch):
+    """cuBLAS DGEMM 8192^3 throughput on this GPU (FP64 peak reference)."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def _model():
+    from mps2_gb300 import hamiltonians as H
+    from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS
+    sv, mpo, qn0, gen = H.heisenberg_chain(L_SITES)
+    mps = FiniteMPS(sv)
+    DirectStateInitMps(mps, H.neel_shuffled_labels(L_SITES, 0), qn0)
+    return mps, mpo
+
+
+def _tensor_bytes(t):
+    return 8 * t.size()
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement timing (oracle) -- test infrastructure used as the baseline
+# ---------------------------------------------------------------------------
+def _oracle_center_update(mpsd, mpo, envs, c, D, iters_cap=None):
+    """Time one 'r' two-site update at site c with the FP64 CPU restatement.
+    mpsd: {site: tensor}, envs: {('l'|'r', len): tensor} (product tensors)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    from oracle.lanczos import LanczosParams as OLP
+    from oracle.vmps import SweepParams as OSP, two_site_update
+    from _convert import to_oracle
+    N = len(mpo)
+    om = [None] * N
+    for k, t in mpsd.items():
+        om[k] = to_oracle(t)
+    oo = [to_oracle(t) if t is not None else None for t in mpo]
+    oe = {k: to_oracle(v) for k, v in envs.items()}
+    lz = OLP(LANCZOS[0], iters_cap + 1 if iters_cap else LANCZOS[1])
+    t0 = time.perf_counter()
+    st = two_site_update(om, oo, oe, OSP(1, D, D, 0.0, lz), "r", c)
+    return time.perf_counter() - t0, st
+
+
+def _synthetic_center_state(fix, seed=0):
+    """Random tensors with the recorded central-bond block structure."""
+    import numpy as np
+    from mps2_gb300.hamiltonians import heisenberg_chain
+    from mps2_gb300.tensor import GQTensor, Index
+    rng = np.random.default_rng(seed)
+    N = fix["L"]
+    c = fix["center"]
+    sv, mpo, qn0, _ = heisenberg_chain(N)
+
+    def idx(d):
+        return Index([(tuple(q), n) for q, n in d["sectors"]], d["dir"])
+
+    def rand(indices, div):
+        t = GQTensor(indices, div)
+        for cc in t.allowed_coords(div):
+            t.blocks[cc] = rng.standard_normal(t.block_shape(cc))
+        return t
+
+    A = rand([idx(d) for d in fix["A_c"]], (0,))
+    B = rand([idx(d) for d in fix["A_c1"]], (0,))
+    Le = rand([idx(d) for d in fix["L"+"_env"]], (0,))
+    Re = rand([idx(d) for d in fix["R_env"]], (0,))
+    return {c: A, c + 1: B}, mpo, {("l", c): Le, ("r", N - c - 2): Re}
+
+
+def _describe_index(ix):
+    return {"dir": ix.dir, "sectors": [[list(q), d] for q, d in ix.sectors()]}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    """CPU restatement on a central update with the recorded structure."""
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    if not os.path.exists(STRUCTURE_FIXTURE):
+        print(json.dumps({"impl": "reference",
+                          "unavailable": "central-bond structure fixture missing"}))
+        return
+    with open(STRUCTURE_FIXTURE) as f:
+        fix = json.load(f)
+    D = fix["D"]
+    c = fix["center"]
+    mpsd, mpo, envs = _synthetic_center_state(fix)
+    times = []
+    for _ in range(args.warmup):
+        _oracle_center_update(dict(mpsd), mpo, dict(envs), c, D, fix["center_iters"])
+    for _ in range(max(1, args.steps)):
+        t, st = _oracle_center_update(dict(mpsd), mpo, dict(envs), c, D, fix["center_iters"])
+        times.append(t)
+    per_update = sum(times) / len(times)
+    sweep_s = per_update * fix["sweep_over_center"]
+    cores = os.cpu_count()
+    line = {
+        "metric": "DMRG sweep time (s/sweep) at D=2000",
+        "value": sweep_s, "unit": "s/sweep", "impl": "reference", "n_gpus": args.gpus,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": per_update * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (random tensors with the central-bond block structure recorded "
+                "from a GPU run of this workload)",
+        "config": {"workload": WORKLOAD, "D": D, "L": fix["L"],
+                   "cache": "inputs larger than L2"},
+        "cpu_baseline": {"value": sweep_s, "unit": "s/sweep", "cores": cores, "kind": "port",
+                         "sample": f"{len(times)} central two-site update(s) at site {c}, "
+                                   f"D={D}, Lanczos capped at {fix['center_iters']} iterations, "
+                                   f"x{fix['sweep_over_center']:.1f} (GPU sweep/update time ratio)"},
+        "e2e": {"value": sweep_s, "unit": "s/sweep", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from mps2_gb300 import _lib
+    from mps2_gb300.vmps import (DMRGState, LanczosParams, SweepParams, library_stream,
+                                 profile_enable, profile_read)
+    _lib.check(_lib.load().gq_init(local))
+    sched = [int(x) for x in args.schedule.split(",")]
+    D = sched[-1]
+    lp = LanczosParams(*LANCZOS)
+
+    def params(d):
+        return SweepParams(1, d, d, 0.0, lp, precision=args.precision)
+
+    mps, mpo = _model()
+    st = DMRGState(mps.tens, mpo)
+    t_setup = time.perf_counter()
+    st.init_envs(args.precision)
+    grow_log = []
+    for d in sched[:-1]:
+        e0, stats = st.sweep(params(d))
+        grow_log.append((d, e0, sum(s.update_seconds for s in stats)))
+        print(f"[setup] sweep at D={d}: E0={e0:.12f} ({grow_log[-1][2]:.1f}s)", file=sys.stderr)
+    for w in range(args.warmup):
+        e0, stats = st.sweep(params(D))
+        print(f"[warmup {w}] D={D} E0={e0:.12f} {sum(s.update_seconds for s in stats):.1f}s",
+              file=sys.stderr)
+    setup_s = time.perf_counter() - t_setup
+
+    ext = torch.cuda.ExternalStream(library_stream())
+    clocks = ClockSampler(local)
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    profile_enable(True)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(ext)
+    timed_stats = []
+    energies = []
+    for k in range(args.steps):
+        e0, stats = st.sweep(params(D))
+        timed_stats.extend(stats)
+        energies.append(e0)
+    ev1.record(ext)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    gemm_key = "gemm_tf32x3" if args.precision == "tf32x3" else "gemm_fp64"
+    g_n, g_ms, g_fl, _ = profile_read(gemm_key)
+    p_n, p_ms, _, p_by = profile_read("permute")
+    v_n, v_ms, _, v_by = profile_read("vector")
+    profile_enable(False)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    sweep_s = ms * 1e-3 / args.steps
+    n_launch_ours = g_n + p_n + v_n
+
+    # ---- end to end through the C ABI from host buffers -------------------
+    host_mps = [st.get_mps(i) for i in range(L_SITES)]
+    host_renv = {n: st.get_env("r", n) for n in range(1, L_SITES - 1)}
+    h2d = sum(_tensor_bytes(t) for t in host_mps) + sum(_tensor_bytes(t) for t in mpo) + \
+        sum(_tensor_bytes(t) for t in host_renv.values())
+    d2h = sum(_tensor_bytes(t) for t in host_mps) + sum(_tensor_bytes(t) for t in host_renv.values())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st2 = DMRGState(host_mps, mpo)
+    for n, t in host_renv.items():
+        st2.set_env("r", n, t)
+    e_e2e, _ = st2.sweep(params(D))
+    out_mps = [st2.get_mps(i) for i in range(L_SITES)]
+    out_env = [st2.get_env("r", n) for n in range(1, L_SITES - 1)]
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    del st2, out_mps, out_env
+
+    # ---- central update: GPU time, structure, CPU restatement --------------
+    c = L_SITES // 2 - 1
+    for i in range(0, c):
+        st.update(params(D), "r", i)
+    center_struct = None
+    mpsd = {c: st.get_mps(c), c + 1: st.get_mps(c + 1)}
+    envs = {("l", c): st.get_env("l", c), ("r", L_SITES - c - 2): st.get_env("r", L_SITES - c - 2)}
+    gpu_center = st.update(params(D), "r", c)
+    sweep_over_center = sweep_s / gpu_center.update_seconds
+    if args.record_structure and rank == 0:
+        center_struct = {
+            "L": L_SITES, "center": c, "D": D, "center_iters": int(gpu_center.iters),
+            "sweep_over_center": sweep_over_center,
+            "A_c": [_describe_index(ix) for ix in mpsd[c].indices],
+            "A_c1": [_describe_index(ix) for ix in mpsd[c + 1].indices],
+            "L_env": [_describe_index(ix) for ix in envs[("l", c)].indices],
+            "R_env": [_describe_index(ix) for ix in envs[("r", L_SITES - c - 2)].indices],
+        }
+        os.makedirs(os.path.dirname(STRUCTURE_FIXTURE), exist_ok=True)
+        with open(STRUCTURE_FIXTURE, "w") as f:
+            json.dump(center_struct, f)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        t_cpu, ost = _oracle_center_update(mpsd, mpo, envs, c, D)
+        cpu = {"value": sweep_s * t_cpu / gpu_center.update_seconds, "unit": "s/sweep",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": (f"1 central two-site update (site {c}, D={D}) of the same state: CPU "
+                          f"{t_cpu:.2f}s vs GPU {gpu_center.update_seconds:.3f}s, scaled by the "
+                          f"GPU sweep time; CPU E0={ost.e0:.12f} GPU E0={gpu_center.e0:.12f}")}
+
+    peaks, peak_kind = _measured_peaks()
+    if args.precision == "fp64":
+        peak = _fp64_peak_tflops(torch)
+        peak_note = "cuBLAS DGEMM 8192^3 measured in this run"
+    else:
+        peak = 0.5 * peaks["bf16_tflops"]
+        peak_note = f"half the {peak_kind} bf16 dense peak (TF32 rate), useful flops"
+    achieved = (g_fl / (g_ms * 1e-3)) / 1e12 if g_ms > 0 else 0.0
+    upd = [s for s in timed_stats]
+    tot = {k: sum(getattr(s, k) for s in upd) for k in
+           ("lanczos_seconds", "svd_seconds", "env_seconds", "update_seconds", "matvec_flops",
+            "env_flops", "matvecs")}
+    line = {
+        "metric": "DMRG sweep time (s/sweep) at D=2000",
+        "value": sweep_s, "unit": "s/sweep", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sweep_s * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "tf32x3 split (f64 sums)",
+        "data": "synthetic model (Heisenberg chain), no dataset",
+        "config": {"workload": WORKLOAD, "L": L_SITES, "D": D, "schedule": sched,
+                   "precision": args.precision, "lanczos": list(LANCZOS),
+                   "parallelism": f"replicas x{ws}", "cache": "inputs larger than L2",
+                   "setup_seconds": setup_s},
+        "energy_last_sweep": energies[-1],
+        "gpu_launches": int(n_launch_ours),
+        "matvec_tflops": tot["matvec_flops"] / tot["lanczos_seconds"] / 1e12
+        if tot["lanczos_seconds"] > 0 else None,
+        "time_split_s": {"lanczos": tot["lanczos_seconds"], "svd": tot["svd_seconds"],
+                         "env": tot["env_seconds"]},
+        "roofline": {"bound": "tensor", "kernel": gemm_key, "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "traffic": None, "peak_source": peak_note, "launches": g_n,
+                     "kernel_ms": g_ms},
+        "vector_ops": {"GB/s": (v_by / (v_ms * 1e-3) / 1e9) if v_ms > 0 else None,
+                       "hbm_peak_gbs": peaks["hbm_gbs"], "launches": v_n},
+        "clocks": clk,
+        "e2e": {"value": e2e_s, "unit": "s/sweep", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

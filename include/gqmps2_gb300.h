@@ -178,9 +178,26 @@ int gq_dmrg_get_env(gq_dmrg *d, int dir, int len, gq_tensor **out);
  * update, the reference's return value. */
 int gq_dmrg_sweep(gq_dmrg *d, const gq_sweep_params *params, gq_update_stats *stats,
                   double *e0);
+/* One two-site update (TwoSiteFiniteVMPSUpdate, :164-340) at `target` in
+ * direction 'r' or 'l'; the caller drives the sweep order. */
+int gq_dmrg_update(gq_dmrg *d, const gq_sweep_params *params, int dir, int target,
+                   gq_update_stats *stats);
 /* Copy of the site tensor i (caller destroys). */
 int gq_dmrg_get_mps(gq_dmrg *d, int i, gq_tensor **out);
 int gq_dmrg_destroy(gq_dmrg *d);
+
+/* Measurement ------------------------------------------------------------ *
+ * Not part of the reference (its only instrumentation is the Timer output,
+ * lanczos_solver_impl.h:123-132).  CUDA-event timing of each kernel family
+ * on the library's stream; enabling resets the counters. */
+#define GQ_PROF_GEMM_FP64 0
+#define GQ_PROF_GEMM_TF32X3 1
+#define GQ_PROF_PERMUTE 2
+#define GQ_PROF_VECTOR 3
+int gq_profile_enable(int on);
+int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes);
+/* The cudaStream_t all library work is queued on. */
+int gq_get_stream(void **stream);
 
 #ifdef __cplusplus
 }

@@ -78,9 +78,15 @@ EXPORTS = {
     "gq_dmrg_set_env": (_I, [_P, _I, _I, _P]),
     "gq_dmrg_get_env": (_I, [_P, _I, _I, _PP]),
     "gq_dmrg_sweep": (_I, [_P, C.POINTER(SweepParamsC), C.POINTER(UpdateStatsC), _DP]),
+    "gq_dmrg_update": (_I, [_P, C.POINTER(SweepParamsC), _I, _I, C.POINTER(UpdateStatsC)]),
     "gq_dmrg_get_mps": (_I, [_P, _I, _PP]),
     "gq_dmrg_destroy": (_I, [_P]),
+    "gq_profile_enable": (_I, [_I]),
+    "gq_profile_read": (_I, [_I, _I64P, _DP, _DP, _DP]),
+    "gq_get_stream": (_I, [_PP]),
 }
+
+PROF = {"gemm_fp64": 0, "gemm_tf32x3": 1, "permute": 2, "vector": 3}
 
 _lib: Optional[C.CDLL] = None
 

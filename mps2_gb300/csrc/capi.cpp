@@ -179,7 +179,7 @@ int gq_contract(const gq_tensor *a, const gq_tensor *b, int naxes, const int *ax
     std::vector<int> xa(axes_a, axes_a + naxes), xb(axes_b, axes_b + naxes);
     double f = 0.0;
     auto c = gq::contract(deref(a, "a"), deref(b, "b"), xa, xb, prec_of(precision), &f);
-    gq::sync();
+    gq::check_device_errors();
     if (flops) *flops = f;
     *out = wrap(c);
   });
@@ -199,7 +199,7 @@ int gq_eff_ham_mul_state(const gq_tensor *L, const gq_tensor *Wl, const gq_tenso
     auto y = gq::clone_structure(*space);
     y->allocate();
     gq::run_matvec(*plan, space->data.p, y->data.p);
-    gq::sync();
+    gq::check_device_errors();
     if (flops) *flops = gq::matvec_flops(*plan);
     *out = wrap(y);
   });
@@ -219,7 +219,7 @@ int gq_lanczos(const gq_tensor *L, const gq_tensor *Wl, const gq_tensor *Wr, con
     lp.error = params->error;
     lp.max_iterations = params->max_iterations;
     auto res = gq::lanczos(h, *space, lp, prec_of(precision));
-    gq::sync();
+    gq::check_device_errors();
     if (iters) *iters = res.iters;
     if (gs_eng) *gs_eng = res.energy;
     if (gs_vec)
@@ -291,19 +291,45 @@ int gq_dmrg_get_env(gq_dmrg *d, int dir, int len, gq_tensor **out) {
   });
 }
 
+namespace {
+gq::SweepParamsC sweep_params(const gq_sweep_params *p) {
+  GQ_CHECK(p, "null sweep parameters");
+  GQ_CHECK(p->sweeps >= 0 && p->dmin >= 1 && p->dmax >= p->dmin, "bad sweep parameters");
+  gq::SweepParamsC sp;
+  sp.sweeps = p->sweeps;
+  sp.dmin = p->dmin;
+  sp.dmax = p->dmax;
+  sp.trunc_err = p->trunc_err;
+  sp.lanczos.error = p->lanczos.error;
+  sp.lanczos.max_iterations = p->lanczos.max_iterations;
+  sp.precision = prec_of(p->precision);
+  sp.verbose = p->verbose;
+  return sp;
+}
+
+void export_stats(const gq::UpdateStatsC &x, gq_update_stats &o) {
+  o.site = x.site;
+  o.dir = x.dir;
+  o.e0 = x.e0;
+  o.trunc_err = x.trunc_err;
+  o.D = x.D;
+  o.iters = x.iters;
+  o.ee = x.ee;
+  o.lanczos_seconds = x.lanczos_seconds;
+  o.update_seconds = x.update_seconds;
+  o.svd_seconds = x.svd_seconds;
+  o.env_seconds = x.env_seconds;
+  o.matvecs = x.matvecs;
+  o.matvec_flops = x.matvec_flops;
+  o.env_flops = x.env_flops;
+  o.theta_size = x.theta_size;
+}
+}  // namespace
+
 int gq_dmrg_sweep(gq_dmrg *d, const gq_sweep_params *p, gq_update_stats *stats, double *e0) {
   return guarded([&] {
-    GQ_CHECK(d && p, "bad arguments");
-    GQ_CHECK(p->sweeps >= 0 && p->dmin >= 1 && p->dmax >= p->dmin, "bad sweep parameters");
-    gq::SweepParamsC sp;
-    sp.sweeps = p->sweeps;
-    sp.dmin = p->dmin;
-    sp.dmax = p->dmax;
-    sp.trunc_err = p->trunc_err;
-    sp.lanczos.error = p->lanczos.error;
-    sp.lanczos.max_iterations = p->lanczos.max_iterations;
-    sp.precision = prec_of(p->precision);
-    sp.verbose = p->verbose;
+    GQ_CHECK(d, "null dmrg handle");
+    const gq::SweepParamsC sp = sweep_params(p);
     double e = 0.0;
     std::vector<gq::UpdateStatsC> st;
     for (int64_t s = 0; s < p->sweeps; ++s) {
@@ -311,28 +337,44 @@ int gq_dmrg_sweep(gq_dmrg *d, const gq_sweep_params *p, gq_update_stats *stats, 
       e = d->d.sweep(sp, &st);
     }
     gq::sync();
-    if (stats) {
-      for (size_t i = 0; i < st.size(); ++i) {
-        gq_update_stats &o = stats[i];
-        const gq::UpdateStatsC &x = st[i];
-        o.site = x.site;
-        o.dir = x.dir;
-        o.e0 = x.e0;
-        o.trunc_err = x.trunc_err;
-        o.D = x.D;
-        o.iters = x.iters;
-        o.ee = x.ee;
-        o.lanczos_seconds = x.lanczos_seconds;
-        o.update_seconds = x.update_seconds;
-        o.svd_seconds = x.svd_seconds;
-        o.env_seconds = x.env_seconds;
-        o.matvecs = x.matvecs;
-        o.matvec_flops = x.matvec_flops;
-        o.env_flops = x.env_flops;
-        o.theta_size = x.theta_size;
-      }
-    }
+    if (stats)
+      for (size_t i = 0; i < st.size(); ++i) export_stats(st[i], stats[i]);
     if (e0) *e0 = e;
+  });
+}
+
+int gq_dmrg_update(gq_dmrg *d, const gq_sweep_params *p, int dir, int target,
+                   gq_update_stats *stats) {
+  return guarded([&] {
+    GQ_CHECK(d, "null dmrg handle");
+    GQ_CHECK(dir == 'r' || dir == 'l', "dir must be 'r' or 'l'");
+    const int N = d->d.N();
+    GQ_CHECK(dir == 'r' ? (target >= 0 && target <= N - 2) : (target >= 1 && target <= N - 1),
+             "target site out of range");
+    auto st = d->d.update(sweep_params(p), (char)dir, target);
+    gq::sync();
+    if (stats) export_stats(st, *stats);
+  });
+}
+
+int gq_profile_enable(int on) {
+  return guarded([&] {
+    gq::ctx();
+    gq::prof_enable(on != 0);
+  });
+}
+
+int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes) {
+  return guarded([&] {
+    GQ_CHECK(kernel >= 0 && kernel < gq::kProfCount, "unknown kernel id");
+    gq::prof_read((gq::ProfKernel)kernel, launches, ms, flops, bytes);
+  });
+}
+
+int gq_get_stream(void **s) {
+  return guarded([&] {
+    GQ_CHECK(s, "null output");
+    *s = (void *)gq::stream();
   });
 }
 

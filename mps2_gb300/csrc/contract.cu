@@ -84,9 +84,11 @@ __global__ void permute_blocks_kernel(const PermBlock *__restrict__ blocks,
 
 void run_perm(const PermPlan &pp, const double *src, double *dst) {
   if (pp.nchunks == 0) return;
+  prof_begin(kProfPermute);
   permute_blocks_kernel<<<(unsigned)pp.nchunks, 256, 0, stream()>>>(pp.blocks.p, pp.chunks.p, src,
                                                                       dst);
   GQ_CUDA(cudaGetLastError());
+  prof_end(kProfPermute, 0.0, 16.0 * (double)pp.total);
 }
 
 }  // namespace
@@ -127,22 +129,6 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   std::vector<int> pa_t = axes_a, pb_t = free_b;
   pa_t.insert(pa_t.end(), free_a.begin(), free_a.end());
   pb_t.insert(pb_t.end(), axes_b.begin(), axes_b.end());
-  if (is_identity(pa)) {
-    plan->transA = 0;
-  } else if (is_identity(pa_t)) {
-    plan->transA = 1;
-  } else {
-    plan->transA = 0;
-    build_perm_plan(a, pa, plan->pa);
-  }
-  if (is_identity(pb)) {
-    plan->transB = 0;
-  } else if (is_identity(pb_t)) {
-    plan->transB = 1;
-  } else {
-    plan->transB = 0;
-    build_perm_plan(b, pb, plan->pb);
-  }
 
   // Group B blocks by their contracted-sector key.
   std::unordered_map<std::string, std::vector<int64_t>> bgroups;
@@ -181,14 +167,58 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
     plan->out = make_structure(a.nq, oidx, odiv, blocks);
   }
   const Tensor &o = *plan->out;
+  const size_t nfa = free_a.size();
 
-  const int TM = gemm_tile_m(prec), TN = gemm_tile_n(prec);
+  // Kernel choice.  The tensor-core form pads every block to 128 x 128 x 32
+  // tiles; it is used when at least 30% of the padded work is useful (the
+  // small MPO contractions, with k and n of a few units, stay on the FP64
+  // kernel where they are memory-bound anyway).
+  if (prec == kTF32x3) {
+    double useful = 0.0, padded = 0.0;
+    for (auto &kv : out) {
+      int64_t m = 1, n = 1;
+      for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
+      for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
+      for (auto &cp : kv.second) {
+        int64_t k = 1;
+        for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
+        useful += 2.0 * m * n * k;
+        padded += 2.0 * ((m + 127) / 128 * 128.0) * ((n + 127) / 128 * 128.0) *
+                  ((k + 31) / 32 * 32.0);
+      }
+    }
+    plan->use_tc = padded > 0.0 && useful >= 0.3 * padded;
+    plan->padded_flops = padded;
+  }
+  if (plan->use_tc) {
+    build_tc_pack(a, free_a, axes_a, plan->ta);
+    build_tc_pack(b, free_b, axes_b, plan->tb);
+  } else {
+    if (is_identity(pa)) {
+      plan->transA = 0;
+    } else if (is_identity(pa_t)) {
+      plan->transA = 1;
+    } else {
+      plan->transA = 0;
+      build_perm_plan(a, pa, plan->pa);
+    }
+    if (is_identity(pb)) {
+      plan->transB = 0;
+    } else if (is_identity(pb_t)) {
+      plan->transB = 1;
+    } else {
+      plan->transB = 0;
+      build_perm_plan(b, pb, plan->pb);
+    }
+  }
+
+  const Precision kern = plan->use_tc ? kTF32x3 : kFP64;
+  const int TM = gemm_tile_m(kern), TN = gemm_tile_n(kern);
   plan->tile_m = TM;
   plan->tile_n = TN;
   std::vector<GemmTile> tiles;
   std::vector<GemmPair> pairs;
   std::vector<char> touched(o.nblocks(), 0);
-  const size_t nfa = free_a.size();
   for (auto &kv : out) {
     const int64_t ob = o.find(kv.first.data());
     GQ_CHECK(ob >= 0, "contraction produces a block missing from the target structure");
@@ -202,8 +232,8 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
       int64_t k = 1;
       for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
       GemmPair gp{};
-      gp.a_off = a.offs[cp.ablk];
-      gp.b_off = b.offs[cp.bblk];
+      gp.a_off = plan->use_tc ? plan->ta.base[cp.ablk] : a.offs[cp.ablk];
+      gp.b_off = plan->use_tc ? plan->tb.base[cp.bblk] : b.offs[cp.bblk];
       gp.k = (int)k;
       gp.lda = (int)(plan->transA ? m : k);
       gp.ldb = (int)(plan->transB ? k : n);
@@ -258,12 +288,54 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   return plan;
 }
 
+namespace {
+int64_t floats_as_doubles(int64_t f) { return (f + 1) / 2 + 8; }  // + slack for alignment
+float *align16(double *p) {
+  return reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(p) + 15) & ~(uintptr_t)15);
+}
+}  // namespace
+
 int64_t contract_scratch(const ContractPlan &p) {
+  if (p.use_tc)
+    return (p.a_cached ? 0 : floats_as_doubles(p.ta.floats)) +
+           (p.b_cached ? 0 : floats_as_doubles(p.tb.floats));
   return (p.pa.needed ? p.pa.total : 0) + (p.pb.needed ? p.pb.total : 0);
 }
 
+void cache_operand(ContractPlan &p, int which, const double *src) {
+  if (!p.use_tc) return;
+  if (which == 0) {
+    p.a_packed.alloc(floats_as_doubles(p.ta.floats));
+    run_tc_pack(p.ta, src, align16(p.a_packed.p));
+    p.a_cached = true;
+  } else {
+    p.b_packed.alloc(floats_as_doubles(p.tb.floats));
+    run_tc_pack(p.tb, src, align16(p.b_packed.p));
+    p.b_cached = true;
+  }
+}
+
 void run_contract(const ContractPlan &p, const double *a, const double *b, double *c,
-                  double *scratch, Precision prec) {
+                  double *scratch, Precision) {
+  if (p.use_tc) {
+    double *s = scratch;
+    const float *A, *B;
+    if (p.a_cached) {
+      A = align16(p.a_packed.p);
+    } else {
+      run_tc_pack(p.ta, a, align16(s));
+      A = align16(s);
+      s += floats_as_doubles(p.ta.floats);
+    }
+    if (p.b_cached) {
+      B = align16(p.b_packed.p);
+    } else {
+      run_tc_pack(p.tb, b, align16(s));
+      B = align16(s);
+    }
+    if (p.ntiles > 0) launch_gemm_tf32x3(p, A, B, c);
+    return;
+  }
   const double *A = a, *B = b;
   double *s = scratch;
   if (p.pa.needed) {
@@ -276,10 +348,17 @@ void run_contract(const ContractPlan &p, const double *a, const double *b, doubl
     B = s;
   }
   if (p.ntiles == 0) return;
-  if (prec == kTF32x3)
-    launch_gemm_tf32x3(p, A, B, c);
-  else
-    launch_gemm_fp64(p, A, B, c);
+  launch_gemm_fp64(p, A, B, c);
+}
+
+void check_device_errors() {
+  int h = 0;
+  GQ_CUDA(cudaMemcpyAsync(&h, tc_error_flag(), sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  sync();
+  if (h != 0) {
+    GQ_CUDA(cudaMemsetAsync(tc_error_flag(), 0, sizeof(int), stream()));
+    fail(kCudaError, "a tensor-core GEMM hit its wait limit and stopped early");
+  }
 }
 
 TensorPtr contract(const Tensor &a, const Tensor &b, const std::vector<int> &axes_a,
@@ -377,6 +456,7 @@ __global__ void __launch_bounds__(256)
 void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, double *C) {
   const unsigned grid = (unsigned)p.ntiles;
   auto s = stream();
+  prof_begin(kProfGemmFp64);
   if (p.transA == 0 && p.transB == 0)
     gemm_fp64_kernel<0, 0><<<grid, 256, 0, s>>>(p.tiles.p, p.pairs.p, A, B, C);
   else if (p.transA == 0 && p.transB == 1)
@@ -386,6 +466,7 @@ void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, d
   else
     gemm_fp64_kernel<1, 1><<<grid, 256, 0, s>>>(p.tiles.p, p.pairs.p, A, B, C);
   GQ_CUDA(cudaGetLastError());
+  prof_end(kProfGemmFp64, p.flops, 8.0 * (double)(p.a_elems + p.b_elems));
 }
 
 }  // namespace gq

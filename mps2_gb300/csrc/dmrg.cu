@@ -166,6 +166,7 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
   sync();
   st.env_seconds = seconds_since(te);
   st.env_flops = f1 + f2 + f3;
+  check_device_errors();
   st.update_seconds = seconds_since(t0);
   if (prm.verbose) {
     std::printf("Site %4d E0 = %20.16f TruncErr = %.2e D = %5lld Iter = %3lld LanczT = %8.3f "

@@ -24,6 +24,20 @@ Context &ctx();
 void init_context(int device);
 void sync();
 
+// Kernel profiling with CUDA events on the library stream (off by default).
+enum ProfKernel : int {
+  kProfGemmFp64 = 0,   // FP64 grouped GEMM
+  kProfGemmTf32 = 1,   // 3xTF32 tcgen05 grouped GEMM
+  kProfPermute = 2,    // block permutes feeding the GEMMs
+  kProfVector = 3,     // Lanczos vector kernels
+  kProfCount = 4,
+};
+bool prof_on();
+void prof_enable(bool on);
+void prof_begin(ProfKernel k);
+void prof_end(ProfKernel k, double flops, double bytes);
+void prof_read(ProfKernel k, int64_t *launches, double *ms, double *flops, double *bytes);
+
 // Arithmetic of the contractions (matvec, environment growth).
 enum Precision : int {
   kFP64 = 0,    // FP64 FMA end to end
@@ -62,10 +76,24 @@ struct PermPlan {
   int64_t nchunks = 0;
 };
 
+// Packed split-precision operand: every block as 128-row x 32-k tiles of
+// TF32 hi then lo, each tile in the tensor-core shared-memory image.
+struct TcPackPlan {
+  std::vector<int64_t> base;  // float offset of each block's packed tiles
+  int64_t floats = 0;
+  int64_t ntasks = 0;
+  DevArray<char> blocks_dev, tasks_dev;
+};
+
 struct ContractPlan {
   TensorPtr out;          // output structure (no data)
   int transA = 0, transB = 0;
   PermPlan pa, pb;
+  bool use_tc = false;    // 3xTF32 tcgen05 kernel (else the FP64 kernel)
+  TcPackPlan ta, tb;
+  bool a_cached = false, b_cached = false;  // constant operand packed once
+  DevBuf a_packed, b_packed;
+  double padded_flops = 0.0;
   DevArray<GemmTile> tiles;
   DevArray<GemmPair> pairs;
   int64_t ntiles = 0;
@@ -90,11 +118,22 @@ void run_contract(const ContractPlan &p, const double *a, const double *b, doubl
 TensorPtr contract(const Tensor &a, const Tensor &b, const std::vector<int> &axes_a,
                    const std::vector<int> &axes_b, Precision prec, double *flops_out = nullptr);
 
+// Pack a constant operand of the plan once (which = 0: A, 1: B); later
+// run_contract calls ignore that operand's pointer.
+void cache_operand(ContractPlan &p, int which, const double *src);
+
 // GEMM kernels (launched by run_contract)
 void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, double *C);
-void launch_gemm_tf32x3(const ContractPlan &p, const double *A, const double *B, double *C);
+void launch_gemm_tf32x3(const ContractPlan &p, const float *A, const float *B, double *C);
+void build_tc_pack(const Tensor &t, const std::vector<int> &row_legs,
+                   const std::vector<int> &k_legs, TcPackPlan &pp);
+void run_tc_pack(const TcPackPlan &pp, const double *src, float *dst);
 int gemm_tile_m(Precision prec);
 int gemm_tile_n(Precision prec);
+// Device-side error word of the tensor-core kernels (bounded waits that ran
+// out); check_device_errors() raises and clears it.
+int *tc_error_flag();
+void check_device_errors();
 
 // ---------------------------------------------------------------------------
 // Vector kernels (vecops.cu).  Scalars live in device memory so the Lanczos

@@ -70,6 +70,10 @@ std::shared_ptr<MatvecPlan> plan_matvec(const EffHam &h, const Tensor &space, Pr
     const Tensor &B = s.bs == -2 ? *s.cb : (s.bs == -1 ? space : *mp->inter[s.bs]);
     const bool last = i + 1 == spec.size();
     auto plan = plan_contract(A, B, s.xa, s.xb, last ? &space : nullptr, prec);
+    // Environments and MPO tensors do not change during the solve: pack
+    // them for the tensor cores once.
+    if (s.as == -2) cache_operand(*plan, 0, s.ca->data.p);
+    if (s.bs == -2) cache_operand(*plan, 1, s.cb->data.p);
     MatvecStep st;
     st.plan = plan;
     st.a_src = s.as;
@@ -156,12 +160,28 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   DevBuf red(dot_scratch_elems());
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
   double *hs = ctx().host_scalars;
-  auto t_mv = clk::duration::zero();
 
   auto matvec = [&](const double *x) {
     run_matvec(*plan, x, last.p);
     res.matvecs++;
     res.matvec_flops += plan->flops;
+  };
+
+  // One host round trip per iteration: right after <v_m, H v_m> the next
+  // recurrence vector gamma_{m+1} and its squared norm are formed on the
+  // device, and both scalars come back together.  If the iteration turns
+  // out to be the last one, that speculative vector is simply unused.
+  auto gamma_step = [&](int64_t m1) {  // bases[m1] = last - a[m1-1] v_{m1-1} - b v_{m1-2}
+    while ((int64_t)bases.size() <= m1) bases.emplace_back(n);
+    dev_lanczos_gamma(last.p, bases[m1 - 1].p, a_dev + (m1 - 1),
+                      m1 >= 2 ? bases[m1 - 2].p : nullptr, m1 >= 2 ? n_dev + (m1 - 1) : nullptr,
+                      true, bases[m1].p, n, n_dev + m1, red.p);
+  };
+  auto fetch2 = [&](int64_t m_a) {  // a[m_a] and nrm2[m_a + 1] -> hs[0], hs[1]
+    GQ_CUDA(cudaMemcpyAsync(hs, a_dev + m_a, sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    GQ_CUDA(cudaMemcpyAsync(hs + 1, n_dev + m_a + 1, sizeof(double), cudaMemcpyDeviceToHost,
+                            stream()));
+    sync();
   };
 
   // v0 = init / |init|
@@ -172,8 +192,10 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   dev_scale_rsqrt(bases[0].p, n, n_dev);
   matvec(bases[0].p);
   dev_dot(bases[0].p, last.p, n, a_dev, red.p);
-  fetch(a_dev, hs, 1);
+  gamma_step(1);
+  fetch2(0);
   a[0] = hs[0];
+  double nrm2_next = hs[1];
   double energy0 = a[0];
 
   auto finish = [&](int64_t nvec, int64_t iters, double energy) {
@@ -196,11 +218,7 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   int64_t m = 0;
   while (true) {
     m += 1;
-    bases.emplace_back(n);
-    dev_lanczos_gamma(last.p, bases[m - 1].p, a_dev + (m - 1), m >= 2 ? bases[m - 2].p : nullptr,
-                      m >= 2 ? n_dev + (m - 1) : nullptr, true, bases[m].p, n, n_dev + m, red.p);
-    fetch(n_dev + m, hs, 1);
-    const double nrm2 = hs[0];
+    const double nrm2 = nrm2_next;
     if (!std::isfinite(nrm2)) fail(kNumericalError, "Lanczos vector became non-finite");
     const double norm_gamma = std::sqrt(nrm2);
     if (norm_gamma == 0.0) {  // invariant subspace found
@@ -212,8 +230,16 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
     dev_scale_rsqrt(bases[m].p, n, n_dev + m);
     matvec(bases[m].p);
     dev_dot(bases[m].p, last.p, n, a_dev + m, red.p);
-    fetch(a_dev + m, hs, 1);
+    const bool more = m + 1 < maxit;
+    if (more) gamma_step(m + 1);
+    if (more) {
+      fetch2(m);
+      nrm2_next = hs[1];
+    } else {
+      fetch(a_dev + m, hs, 1);
+    }
     a[m] = hs[0];
+    if (!std::isfinite(a[m])) fail(kNumericalError, "Lanczos coefficient became non-finite");
     double e_new;
     if (!tridiag_lowest(a.data(), b.data(), (int)(m + 1), &e_new, nullptr))
       fail(kNumericalError, "tridiagonal eigensolver did not converge");
@@ -223,7 +249,6 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
     }
     energy0 = e_new;
   }
-  (void)t_mv;
   return res;
 }
 

@@ -44,6 +44,7 @@ void init_context(int device) {
   GQ_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
   GQ_CUDA(cudaMallocHost((void **)&c->host_scalars, sizeof(double) * 64));
   GQ_CUDA(cudaMallocAsync((void **)&c->dev_scalars, sizeof(double) * 64, c->stream));
+  GQ_CUDA(cudaMemsetAsync(c->dev_scalars, 0, sizeof(double) * 64, c->stream));
   GQ_CUDA(cudaEventCreateWithFlags(&c->sync_event, cudaEventDisableTiming));
   g_ctx = c;
 }
@@ -63,6 +64,83 @@ void DevBuf::release() {
   if (p) cudaFreeAsync(p, stream());
   p = nullptr;
   n = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel profiling
+// ---------------------------------------------------------------------------
+namespace {
+struct ProfRec { int k; cudaEvent_t e0, e1; double flops, bytes; };
+struct ProfState {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<ProfRec> pending;
+  cudaEvent_t open[kProfCount] = {};
+  int64_t launches[kProfCount] = {};
+  double ms[kProfCount] = {}, flops[kProfCount] = {}, bytes[kProfCount] = {};
+} g_prof;
+
+cudaEvent_t prof_event() {
+  if (!g_prof.pool.empty()) {
+    auto e = g_prof.pool.back();
+    g_prof.pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  GQ_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void prof_drain() {
+  if (g_prof.pending.empty()) return;
+  sync();
+  for (auto &r : g_prof.pending) {
+    float t = 0.f;
+    GQ_CUDA(cudaEventElapsedTime(&t, r.e0, r.e1));
+    g_prof.launches[r.k]++;
+    g_prof.ms[r.k] += t;
+    g_prof.flops[r.k] += r.flops;
+    g_prof.bytes[r.k] += r.bytes;
+    g_prof.pool.push_back(r.e0);
+    g_prof.pool.push_back(r.e1);
+  }
+  g_prof.pending.clear();
+}
+}  // namespace
+
+bool prof_on() { return g_prof.on; }
+
+void prof_enable(bool on) {
+  prof_drain();
+  for (int k = 0; k < kProfCount; ++k) {
+    g_prof.launches[k] = 0;
+    g_prof.ms[k] = g_prof.flops[k] = g_prof.bytes[k] = 0.0;
+  }
+  g_prof.on = on;
+}
+
+void prof_begin(ProfKernel k) {
+  if (!g_prof.on) return;
+  auto e = prof_event();
+  GQ_CUDA(cudaEventRecord(e, stream()));
+  g_prof.open[k] = e;
+}
+
+void prof_end(ProfKernel k, double flops, double bytes) {
+  if (!g_prof.on || !g_prof.open[k]) return;
+  auto e = prof_event();
+  GQ_CUDA(cudaEventRecord(e, stream()));
+  g_prof.pending.push_back({(int)k, g_prof.open[k], e, flops, bytes});
+  g_prof.open[k] = nullptr;
+  if (g_prof.pending.size() > 4096) prof_drain();
+}
+
+void prof_read(ProfKernel k, int64_t *launches, double *ms, double *flops, double *bytes) {
+  prof_drain();
+  if (launches) *launches = g_prof.launches[k];
+  if (ms) *ms = g_prof.ms[k];
+  if (flops) *flops = g_prof.flops[k];
+  if (bytes) *bytes = g_prof.bytes[k];
 }
 
 // ---------------------------------------------------------------------------

@@ -15,10 +15,11 @@
 //    sum_{i>=D} s_i^2 / sum s^2 <= trunc_err, capped by Dmax and #values;
 //  * kept nonzero values use the solver's vectors with the largest-|.|
 //    entry of each left vector made positive (right vector follows); kept
-//    zero values use the canonical completion: columns r.. of the complete
-//    Householder-QR orthogonal factor of the group's nonzero singular
-//    vectors (geqrf + ormqr);
+//    zero values use the canonical completion of null_completion (a
+//    counter-hashed seed matrix projected off the group's nonzero singular
+//    vectors, then CholeskyQR2);
 //  * new bond sectors: groups with a kept value, ascending charge.
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <map>
@@ -135,14 +136,40 @@ __global__ void scatter_kernel(const ScatterItem *__restrict__ items,
   }
 }
 
-__global__ void unit_cols_kernel(double *__restrict__ c, int m, int r, int k) {
-  // c (m x k col-major) = [0_{r x k}; I_k; 0]
-  const int64_t n = (int64_t)m * k;
+// Counter-based seed matrix for the null-space completion: element (i, j) =
+// splitmix64(key ^ (i << 20) ^ j), top 53 bits scaled by 2^-53, minus 0.5.
+// Every operation is exact, so the CPU oracle reproduces it bit for bit.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  unsigned long long z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void seed_matrix_kernel(double *__restrict__ w, int dim, int k,
+                                   unsigned long long key) {
+  const int64_t n = (int64_t)dim * k;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int row = (int)(e % m), col = (int)(e / m);
-    c[e] = row == r + col ? 1.0 : 0.0;
+    const unsigned long long i = (unsigned long long)(e % dim), j = (unsigned long long)(e / dim);
+    const unsigned long long z = splitmix64(key ^ (i << 20) ^ j);
+    w[e] = (double)(z >> 11) * 0x1p-53 - 0.5;
   }
+}
+
+#define GQ_BLAS(call)                                                                 \
+  do {                                                                                \
+    cublasStatus_t s_ = (call);                                                       \
+    if (s_ != CUBLAS_STATUS_SUCCESS)                                                  \
+      ::gq::fail(::gq::kSolverError, std::string(#call) + " failed with status " +    \
+                                         std::to_string((int)s_));                    \
+  } while (0)
+
+cublasHandle_t blas() {
+  static cublasHandle_t h = nullptr;
+  if (!h) GQ_BLAS(cublasCreate(&h));
+  GQ_BLAS(cublasSetStream(h, stream()));
+  return h;
 }
 
 struct Group {
@@ -157,33 +184,51 @@ struct Group {
   int64_t lc_off = 0, rc_off = 0;  // completion buffers
 };
 
-// Canonical completion: first k columns orthogonal to the r orthonormal
-// columns of `vecs` (dim x r, col-major, ld dim), written to out (dim x k).
-void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, double *out) {
+// Canonical completion: k orthonormal columns orthogonal to the r
+// orthonormal columns of `vecs` (dim x r, col-major, ld dim), written to
+// out (dim x k, col-major).  The seed matrix is projected off `vecs` twice
+// (Gram-Schmidt with re-orthogonalisation) and orthonormalised by
+// CholeskyQR2; nothing depends on the signs of the columns of `vecs`.
+void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, int group, int side,
+                     double *out) {
   if (k == 0) return;
   auto s = stream();
   const unsigned grid = (unsigned)std::min<int64_t>((dim * k + 255) / 256, 4096);
-  unit_cols_kernel<<<grid, 256, 0, s>>>(out, (int)dim, (int)r, (int)k);
+  const unsigned long long key = (unsigned long long)(2 * group + side) << 40;
+  seed_matrix_kernel<<<grid, 256, 0, s>>>(out, (int)dim, (int)k, key);
   GQ_CUDA(cudaGetLastError());
-  if (r == 0) return;
-  auto h = solver();
-  DevBuf a(dim * r), tau(r);
-  GQ_CUDA(cudaMemcpyAsync(a.p, vecs, sizeof(double) * dim * r, cudaMemcpyDeviceToDevice, s));
-  int lw1 = 0, lw2 = 0;
-  GQ_SOLVER(cusolverDnDgeqrf_bufferSize(h, (int)dim, (int)r, a.p, (int)dim, &lw1));
-  GQ_SOLVER(cusolverDnDormqr_bufferSize(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, (int)dim, (int)k, (int)r,
-                                        a.p, (int)dim, tau.p, out, (int)dim, &lw2));
-  DevBuf work(std::max(lw1, lw2) + 1);
-  int *info = nullptr;
-  GQ_CUDA(cudaMallocAsync((void **)&info, sizeof(int), s));
-  GQ_SOLVER(cusolverDnDgeqrf(h, (int)dim, (int)r, a.p, (int)dim, tau.p, work.p, lw1, info));
-  GQ_SOLVER(cusolverDnDormqr(h, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, (int)dim, (int)k, (int)r, a.p,
-                             (int)dim, tau.p, out, (int)dim, work.p, lw2, info));
-  int hinfo = 0;
-  GQ_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s));
-  GQ_CUDA(cudaFreeAsync(info, s));
+  auto bh = blas();
+  const int d = (int)dim, kk = (int)k, rr = (int)r;
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  if (r > 0) {
+    DevBuf t(r * k);
+    for (int pass = 0; pass < 2; ++pass) {
+      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, rr, kk, d, &one, vecs, d, out, d, &zero,
+                          t.p, rr));
+      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, d, kk, rr, &mone, vecs, d, t.p, rr, &one,
+                          out, d));
+    }
+  }
+  auto sh = solver();
+  DevBuf g(k * k);
+  int lw = 0;
+  GQ_SOLVER(cusolverDnDpotrf_bufferSize(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, &lw));
+  DevBuf work((int64_t)lw + 1);
+  DevArray<int> info;
+  info.upload(std::vector<int>(2, 0));
+  for (int pass = 0; pass < 2; ++pass) {
+    GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, kk, kk, d, &one, out, d, out, d, &zero, g.p,
+                        kk));
+    GQ_SOLVER(cusolverDnDpotrf(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, work.p, lw,
+                               info.p + pass));
+    GQ_BLAS(cublasDtrsm(bh, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                        CUBLAS_DIAG_NON_UNIT, d, kk, &one, g.p, kk, out, d));
+  }
+  int hinfo[2] = {0, 0};
+  GQ_CUDA(cudaMemcpyAsync(hinfo, info.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
   sync();
-  if (hinfo != 0) fail(kSolverError, "QR completion failed, info=" + std::to_string(hinfo));
+  if (hinfo[0] != 0 || hinfo[1] != 0)
+    fail(kSolverError, "null-space completion: Cholesky failed");
 }
 }  // namespace
 
@@ -390,8 +435,9 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   for (Group *g : groups) {
     const int64_t kz = g->keep - g->keep_nz;
     if (kz == 0) continue;
-    null_completion(lv.p + g->lv_off, g->m, g->nnz, kz, lcomp.p + g->lc_off);
-    null_completion(rv.p + g->rv_off, g->n, g->nnz, kz, rcomp.p + g->rc_off);
+    const int gidx = (int)(std::find(groups.begin(), groups.end(), g) - groups.begin());
+    null_completion(lv.p + g->lv_off, g->m, g->nnz, kz, gidx, 0, lcomp.p + g->lc_off);
+    null_completion(rv.p + g->rv_off, g->n, g->nnz, kz, gidx, 1, rcomp.p + g->rc_off);
   }
 
   // ---- output tensors --------------------------------------------------------

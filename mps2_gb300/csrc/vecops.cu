@@ -120,23 +120,29 @@ unsigned stream_grid(int64_t n) {
 int64_t dot_scratch_elems() { return kRedBlocks; }
 
 void dev_dot(const double *x, const double *y, int64_t n, double *out_dev, double *scratch) {
+  prof_begin(kProfVector);
   dot_partial_kernel<<<kRedBlocks, kRedThreads, 0, stream()>>>(x, y, n, scratch);
   finish_sum_kernel<<<1, kRedThreads, 0, stream()>>>(scratch, kRedBlocks, out_dev);
   GQ_CUDA(cudaGetLastError());
+  prof_end(kProfVector, 2.0 * n, 16.0 * n);
 }
 
 void dev_lanczos_gamma(const double *x, const double *u, const double *a_dev, const double *v,
                        const double *b_dev, bool b_is_sq, double *y, int64_t n,
                        double *nrm2_out_dev, double *scratch) {
+  prof_begin(kProfVector);
   gamma_kernel<<<kRedBlocks, kRedThreads, 0, stream()>>>(x, u, a_dev, v, b_dev, b_is_sq ? 1 : 0,
                                                          y, n, scratch);
   finish_sum_kernel<<<1, kRedThreads, 0, stream()>>>(scratch, kRedBlocks, nrm2_out_dev);
   GQ_CUDA(cudaGetLastError());
+  prof_end(kProfVector, 6.0 * n, 8.0 * n * (2 + (u ? 1 : 0) + (v ? 1 : 0)));
 }
 
 void dev_scale_rsqrt(double *x, int64_t n, const double *nrm2_dev) {
+  prof_begin(kProfVector);
   scale_rsqrt_kernel<<<stream_grid(n), 256, 0, stream()>>>(x, n, nrm2_dev);
   GQ_CUDA(cudaGetLastError());
+  prof_end(kProfVector, (double)n, 16.0 * n);
 }
 
 void dev_scale(double *x, int64_t n, double s) {
@@ -151,8 +157,10 @@ void dev_combine(const std::vector<const double *> &bases, const std::vector<dou
   DevArray<double> dc;
   dp.upload(bases);
   dc.upload(c);
+  prof_begin(kProfVector);
   combine_kernel<<<stream_grid(n), 256, 0, stream()>>>(dp.p, dc.p, m, out, n);
   GQ_CUDA(cudaGetLastError());
+  prof_end(kProfVector, 2.0 * n * m, 8.0 * n * (m + 1));
 }
 
 void dev_block_copy(const double *src, double *dst, const std::vector<int64_t> &triples) {

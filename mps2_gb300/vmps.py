@@ -123,6 +123,12 @@ class DMRGState:
         check(load().gq_dmrg_sweep(self.h, C.byref(pc), stats, C.byref(e0)))
         return e0.value, [UpdateStats(stats[i]) for i in range(2 * (self.N - 1) * ns)]
 
+    def update(self, params: SweepParams, dir: str, target: int) -> UpdateStats:
+        st = _lib.UpdateStatsC()
+        pc = params.to_c(1)
+        check(load().gq_dmrg_update(self.h, C.byref(pc), ord(dir), int(target), C.byref(st)))
+        return UpdateStats(st)
+
     def get_mps(self, i: int) -> GQTensor:
         out = C.c_void_p()
         check(load().gq_dmrg_get_mps(self.h, int(i), C.byref(out)))
@@ -160,6 +166,25 @@ def TwoSiteFiniteVMPS(mps: FiniteMPS, mpo: Sequence[GQTensor], sweep_params: Swe
         write_tensor(st.get_env("r", length), GenEnvTenName("r", length, sp.temp_path))
     mps.clear()
     return e0
+
+
+def profile_enable(on: bool = True) -> None:
+    check(load().gq_profile_enable(1 if on else 0))
+
+
+def profile_read(kernel: str):
+    """(launches, total ms, flops, bytes) of one kernel family since the
+    last :func:`profile_enable`."""
+    n, ms, fl, by = C.c_int64(), C.c_double(), C.c_double(), C.c_double()
+    check(load().gq_profile_read(_lib.PROF[kernel], C.byref(n), C.byref(ms), C.byref(fl),
+                                 C.byref(by)))
+    return n.value, ms.value, fl.value, by.value
+
+
+def library_stream() -> int:
+    s = C.c_void_p()
+    check(load().gq_get_stream(C.byref(s)))
+    return s.value or 0
 
 
 class LanczosRes:

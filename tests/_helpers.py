@@ -19,11 +19,23 @@ def random_index(rng, nsec, qrange, dmax, dir, nq=1):
 
 
 def random_tensor(rng, indices, div, fill=1.0):
+    """Random blocks on a `fill` fraction of the allowed blocks (at least
+    one block whenever the divergence allows any)."""
     t = GQTensor(indices, div)
-    for c in t.allowed_coords(div):
+    allowed = t.allowed_coords(div)
+    for c in allowed:
         if rng.random() <= fill:
             t.blocks[c] = rng.standard_normal(t.block_shape(c))
+    if allowed and not t.blocks:
+        c = allowed[int(rng.integers(len(allowed)))]
+        t.blocks[c] = rng.standard_normal(t.block_shape(c))
     return t
+
+
+def first_allowed_div(indices):
+    """A divergence for which these legs allow at least one block."""
+    t = GQTensor(indices)
+    return t.block_div(tuple(0 for _ in indices))
 
 
 def rel_err(gpu: GQTensor, ref) -> float:

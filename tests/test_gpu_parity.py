@@ -15,7 +15,7 @@ from mps2_gb300 import hamiltonians as H
 from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS
 from mps2_gb300.tensor import GQTensor, IN, OUT
 from _convert import from_oracle, to_oracle
-from _helpers import oracle_state, random_index, random_tensor, rel_err
+from _helpers import first_allowed_div, oracle_state, random_index, random_tensor, rel_err
 from golden_cases import cases
 
 pytestmark = pytest.mark.gpu
@@ -59,12 +59,8 @@ def test_contract_matches_oracle(lib, case):
     ib = [random_index(rng, 3, 2, 5, OUT if rng.random() < 0.5 else IN) for _ in range(rb)]
     for a_ax, b_ax in zip(xa, xb):
         ib[b_ax] = ia[a_ax].inverse()
-    a = random_tensor(rng, ia, (0,), fill=0.8)
-    from mps2_gb300.tensor import GQTensor
-    cands = GQTensor(ib).allowed_coords((1,)) or [None]
-    bdiv = (1,) if cands[0] is not None else GQTensor(ib).block_div(
-        tuple(0 for _ in ib))
-    b = random_tensor(rng, ib, bdiv, fill=0.8)
+    a = random_tensor(rng, ia, first_allowed_div(ia), fill=0.8)
+    b = random_tensor(rng, ib, first_allowed_div(ib), fill=0.8)
     assert a.blocks and b.blocks
     ref = oracle.contract(to_oracle(a), to_oracle(b), xa, xb)
     got = Contract(a, b, (xa, xb))
