@@ -134,6 +134,24 @@ int gq_tensor_destroy(gq_tensor *t);
 int gq_contract(const gq_tensor *a, const gq_tensor *b, int naxes, const int *axes_a,
                 const int *axes_b, int precision, gq_tensor **out, double *flops);
 
+/* Contraction without device allocation.  This entry point has no
+ * counterpart in the reference.  It serves callers that own all device
+ * memory themselves and cannot let a library allocate during their work (a
+ * host application that lends the library a fixed budget, a plugin inside
+ * another framework's time step, where cudaMalloc's device-wide
+ * synchronisation would stall unrelated work).  Same result as gq_contract
+ * with GQ_PREC_FP64, written into `out`, which the caller creates beforehand
+ * (gq_tensor_create) with a's free legs then b's free legs, divergence
+ * div(a) + div(b), and every block the contraction produces.  Scratch lives
+ * in arrays the library reserves on each GPU when it is loaded (about
+ * 22 MiB, kept until exit): a and b together may hold at most 2^21
+ * elements, with at most 2^15 output tiles of 64 x 64, 2^17 block products
+ * and 2^15 permute tasks; larger inputs return GQ_ERR_INVALID.  The first
+ * call on a device looks the arrays up (do it before any stream capture).
+ * Calls share the arrays: calls that overlap on the GPU race. */
+int gq_contract_noalloc(const gq_tensor *a, const gq_tensor *b, int naxes, const int *axes_a,
+                        const int *axes_b, gq_tensor *out);
+
 /* Effective Hamiltonian ------------------------------------------------- *
  * eff_ham_mul_state_{cent,lend,rend} (lanczos_solver_impl.h:228-256).
  * L / R may be NULL at the chain ends (where = LEND / REND).  The result

@@ -70,6 +70,7 @@ EXPORTS = {
     "gq_tensor_export": (_I, [_P, _IP, _IP, _IP, _I64P, _IP, _IP, _DP]),
     "gq_tensor_destroy": (_I, [_P]),
     "gq_contract": (_I, [_P, _P, _I, _IP, _IP, _I, _PP, _DP]),
+    "gq_contract_noalloc": (_I, [_P, _P, _I, _IP, _IP, _P]),
     "gq_eff_ham_mul_state": (_I, [_P, _P, _P, _P, _I, _P, _I, _PP, _DP]),
     "gq_lanczos": (_I, [_P, _P, _P, _P, _I, _P, C.POINTER(LanczosParamsC), _I, _I64P, _DP, _PP]),
     "gq_svd": (_I, [_P, _I, _IP, _D, _I64, _I64, _I, _PP, _PP, _DP, _I64, _DP, _I64P]),

@@ -185,6 +185,15 @@ int gq_contract(const gq_tensor *a, const gq_tensor *b, int naxes, const int *ax
   });
 }
 
+int gq_contract_noalloc(const gq_tensor *a, const gq_tensor *b, int naxes, const int *axes_a,
+                        const int *axes_b, gq_tensor *out) {
+  return guarded([&] {
+    GQ_CHECK(out && out->t && axes_a && axes_b && naxes >= 1, "bad arguments");
+    std::vector<int> xa(axes_a, axes_a + naxes), xb(axes_b, axes_b + naxes);
+    gq::contract_noalloc(deref(a, "a"), deref(b, "b"), xa, xb, *out->t);
+  });
+}
+
 int gq_eff_ham_mul_state(const gq_tensor *L, const gq_tensor *Wl, const gq_tensor *Wr,
                          const gq_tensor *R, int where, const gq_tensor *state, int precision,
                          gq_tensor **out, double *flops) {

@@ -135,6 +135,11 @@ int gemm_tile_n(Precision prec);
 int *tc_error_flag();
 void check_device_errors();
 
+// FP64 contraction into a caller-created output without any device
+// allocation (noalloc.cu).
+void contract_noalloc(const Tensor &a, const Tensor &b, const std::vector<int> &axes_a,
+                      const std::vector<int> &axes_b, Tensor &out);
+
 // ---------------------------------------------------------------------------
 // Vector kernels (vecops.cu).  Scalars live in device memory so the Lanczos
 // recurrence runs without a host round trip per operation.
