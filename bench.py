@@ -53,7 +53,7 @@ def _args():
     p.add_argument("--steps", type=int, default=1)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--precision", choices=["fp64", "tf32x3"], default="fp64")
+    p.add_argument("--precision", choices=["fp64", "tf32x3"], default="tf32x3")
     p.add_argument("--schedule", default=",".join(map(str, SCHEDULE)),
                    help="comma-separated D per growth sweep; the last is the timed D")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -266,31 +266,31 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     from mps2_gb300 import _lib
-    from mps2_gb300.vmps import (DMRGState, LanczosParams, SweepParams, library_stream,
-                                 profile_enable, profile_read)
+    from mps2_gb300.vmps import (Contract, DMRGState, LanczosParams, LanczosSolver, SweepParams,
+                                 library_stream, profile_enable, profile_read)
     _lib.check(_lib.load().gq_init(local))
     sched = [int(x) for x in args.schedule.split(",")]
     D = sched[-1]
     lp = LanczosParams(*LANCZOS)
 
-    def params(d):
-        return SweepParams(1, d, d, 0.0, lp, precision=args.precision)
+    def params(d, prec=args.precision):
+        return SweepParams(1, d, d, 0.0, lp, precision=prec)
 
     mps, mpo = _model()
     st = DMRGState(mps.tens, mpo)
     t_setup = time.perf_counter()
     st.init_envs(args.precision)
-    grow_log = []
     for d in sched[:-1]:
         e0, stats = st.sweep(params(d))
-        grow_log.append((d, e0, sum(s.update_seconds for s in stats)))
-        print(f"[setup] sweep at D={d}: E0={e0:.12f} ({grow_log[-1][2]:.1f}s)", file=sys.stderr)
+        print(f"[setup] sweep at D={d}: E0={e0:.12f} max bond {max(x.D for x in stats)} "
+              f"({sum(x.update_seconds for x in stats):.1f}s)", file=sys.stderr)
     for w in range(args.warmup):
         e0, stats = st.sweep(params(D))
-        print(f"[warmup {w}] D={D} E0={e0:.12f} {sum(s.update_seconds for s in stats):.1f}s",
+        print(f"[warmup {w}] D={D} E0={e0:.12f} {sum(x.update_seconds for x in stats):.1f}s",
               file=sys.stderr)
     setup_s = time.perf_counter() - t_setup
 
+    # ---- timed sweeps -------------------------------------------------------
     ext = torch.cuda.ExternalStream(library_stream())
     clocks = ClockSampler(local)
     if ws > 1:
@@ -301,8 +301,7 @@ def run_ours(args):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(ext)
-    timed_stats = []
-    energies = []
+    timed_stats, energies = [], []
     for k in range(args.steps):
         e0, stats = st.sweep(params(D))
         timed_stats.extend(stats)
@@ -311,19 +310,16 @@ def run_ours(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
-    gemm_key = "gemm_tf32x3" if args.precision == "tf32x3" else "gemm_fp64"
-    g_n, g_ms, g_fl, _ = profile_read(gemm_key)
-    p_n, p_ms, _, p_by = profile_read("permute")
-    v_n, v_ms, _, v_by = profile_read("vector")
+    prof = {k: profile_read(k) for k in ("gemm_fp64", "gemm_tf32x3", "permute", "vector")}
     profile_enable(False)
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     sweep_s = ms * 1e-3 / args.steps
-    n_launch_ours = g_n + p_n + v_n
+    n_launch_ours = sum(v[0] for v in prof.values())
 
-    # ---- end to end through the C ABI from host buffers -------------------
+    # ---- end to end through the C ABI from host buffers ---------------------
     host_mps = [st.get_mps(i) for i in range(L_SITES)]
     host_renv = {n: st.get_env("r", n) for n in range(1, L_SITES - 1)}
     h2d = sum(_tensor_bytes(t) for t in host_mps) + sum(_tensor_bytes(t) for t in mpo) + \
@@ -334,26 +330,43 @@ def run_ours(args):
     st2 = DMRGState(host_mps, mpo)
     for n, t in host_renv.items():
         st2.set_env("r", n, t)
-    e_e2e, _ = st2.sweep(params(D))
+    st2.sweep(params(D))
     out_mps = [st2.get_mps(i) for i in range(L_SITES)]
     out_env = [st2.get_env("r", n) for n in range(1, L_SITES - 1)]
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     del st2, out_mps, out_env
 
-    # ---- central update: GPU time, structure, CPU restatement --------------
+    # ---- the central two-site problem: FP64 vs split, CPU restatement ------
     c = L_SITES // 2 - 1
     for i in range(0, c):
         st.update(params(D), "r", i)
-    center_struct = None
     mpsd = {c: st.get_mps(c), c + 1: st.get_mps(c + 1)}
     envs = {("l", c): st.get_env("l", c), ("r", L_SITES - c - 2): st.get_env("r", L_SITES - c - 2)}
+    theta = Contract(mpsd[c], mpsd[c + 1], ([2], [0]))
+    eff = [envs[("l", c)], mpo[c], mpo[c + 1], envs[("r", L_SITES - c - 2)]]
+    solve = {}
+    for prec in ("fp64", "tf32x3"):
+        profile_enable(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = LanczosSolver(eff, theta, lp, "cent", precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        pr = {k: profile_read(k) for k in ("gemm_fp64", "gemm_tf32x3", "permute", "vector")}
+        profile_enable(False)
+        gemm_ms = pr["gemm_fp64"][1] + pr["gemm_tf32x3"][1]
+        gemm_fl = pr["gemm_fp64"][2] + pr["gemm_tf32x3"][2]
+        solve[prec] = {"energy": r.gs_eng, "iters": r.iters, "seconds": dt,
+                       "matvec_gemm_tflops": gemm_fl / (gemm_ms * 1e-3) / 1e12 if gemm_ms else None,
+                       "tc_gemm_tflops": (pr["gemm_tf32x3"][2] / (pr["gemm_tf32x3"][1] * 1e-3) / 1e12
+                                          if pr["gemm_tf32x3"][1] else None)}
+    de = abs(solve["tf32x3"]["energy"] - solve["fp64"]["energy"]) / abs(solve["fp64"]["energy"])
     gpu_center = st.update(params(D), "r", c)
-    sweep_over_center = sweep_s / gpu_center.update_seconds
     if args.record_structure and rank == 0:
         center_struct = {
-            "L": L_SITES, "center": c, "D": D, "center_iters": int(gpu_center.iters),
-            "sweep_over_center": sweep_over_center,
+            "L": L_SITES, "center": c, "D": D, "center_iters": int(max(1, gpu_center.iters)),
+            "sweep_over_center": sweep_s / gpu_center.update_seconds,
             "A_c": [_describe_index(ix) for ix in mpsd[c].indices],
             "A_c1": [_describe_index(ix) for ix in mpsd[c + 1].indices],
             "L_env": [_describe_index(ix) for ix in envs[("l", c)].indices],
@@ -371,24 +384,30 @@ def run_ours(args):
                           f"{t_cpu:.2f}s vs GPU {gpu_center.update_seconds:.3f}s, scaled by the "
                           f"GPU sweep time; CPU E0={ost.e0:.12f} GPU E0={gpu_center.e0:.12f}")}
 
+    # ---- roofline of the dominant kernel family ------------------------------
     peaks, peak_kind = _measured_peaks()
-    if args.precision == "fp64":
-        peak = _fp64_peak_tflops(torch)
-        peak_note = "cuBLAS DGEMM 8192^3 measured in this run"
-    else:
-        peak = 0.5 * peaks["bf16_tflops"]
-        peak_note = f"half the {peak_kind} bf16 dense peak (TF32 rate), useful flops"
-    achieved = (g_fl / (g_ms * 1e-3)) / 1e12 if g_ms > 0 else 0.0
-    upd = [s for s in timed_stats]
-    tot = {k: sum(getattr(s, k) for s in upd) for k in
+    fp64_peak = _fp64_peak_tflops(torch)
+    fam = {"gemm_tf32x3": ("tensor", "TFLOP/s", 0.5 * peaks["bf16_tflops"],
+                           f"half the {peak_kind} bf16 dense peak (the TF32 rate); useful flops"),
+           "gemm_fp64": ("fp64", "TFLOP/s", fp64_peak, "cuBLAS DGEMM 8192^3 measured in this run"),
+           "permute": ("hbm", "GB/s", peaks["hbm_gbs"], f"{peak_kind} HBM copy bandwidth"),
+           "vector": ("hbm", "GB/s", peaks["hbm_gbs"], f"{peak_kind} HBM copy bandwidth")}
+    top = max(prof, key=lambda k: prof[k][1])
+    n_l, t_ms, fl, by = prof[top]
+    bound, unit, peak, note = fam[top]
+    achieved = ((fl / 1e12) if unit == "TFLOP/s" else (by / 1e9)) / (t_ms * 1e-3) if t_ms else 0.0
+    kernels = {k: {"launches": v[0], "ms": v[1],
+                   "share_of_sweep": v[1] * 1e-3 / (sweep_s * args.steps)} for k, v in prof.items()}
+    tot = {k: sum(getattr(s, k) for s in timed_stats) for k in
            ("lanczos_seconds", "svd_seconds", "env_seconds", "update_seconds", "matvec_flops",
             "env_flops", "matvecs")}
+    u64 = gpu_center.update_seconds - gpu_center.lanczos_seconds + solve["fp64"]["seconds"]
     line = {
         "metric": "DMRG sweep time (s/sweep) at D=2000",
         "value": sweep_s, "unit": "s/sweep", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sweep_s * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "tf32x3 split (f64 sums)",
+        "dtype": "f64" if args.precision == "fp64" else "tf32x3 split products, f64 sums",
         "data": "synthetic model (Heisenberg chain), no dataset",
         "config": {"workload": WORKLOAD, "L": L_SITES, "D": D, "schedule": sched,
                    "precision": args.precision, "lanczos": list(LANCZOS),
@@ -396,16 +415,15 @@ def run_ours(args):
                    "setup_seconds": setup_s},
         "energy_last_sweep": energies[-1],
         "gpu_launches": int(n_launch_ours),
-        "matvec_tflops": tot["matvec_flops"] / tot["lanczos_seconds"] / 1e12
-        if tot["lanczos_seconds"] > 0 else None,
         "time_split_s": {"lanczos": tot["lanczos_seconds"], "svd": tot["svd_seconds"],
-                         "env": tot["env_seconds"]},
-        "roofline": {"bound": "tensor", "kernel": gemm_key, "achieved": achieved, "peak": peak,
-                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "traffic": None, "peak_source": peak_note, "launches": g_n,
-                     "kernel_ms": g_ms},
-        "vector_ops": {"GB/s": (v_by / (v_ms * 1e-3) / 1e9) if v_ms > 0 else None,
-                       "hbm_peak_gbs": peaks["hbm_gbs"], "launches": v_n},
+                         "env": tot["env_seconds"], "matvecs": tot["matvecs"]},
+        "central_problem": {"fp64": solve["fp64"], "tf32x3": solve["tf32x3"],
+                            "delta_e_rel": de,
+                            "fp64_sweep_s_est": sweep_s * u64 / gpu_center.update_seconds},
+        "kernels": kernels,
+        "roofline": {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak,
+                     "unit": unit, "frac": achieved / peak if peak else None, "traffic": None,
+                     "peak_source": note, "launches": n_l, "kernel_ms": t_ms},
         "clocks": clk,
         "e2e": {"value": e2e_s, "unit": "s/sweep", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

@@ -169,16 +169,113 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   const Tensor &o = *plan->out;
   const size_t nfa = free_a.size();
 
-  // Kernel choice.  The tensor-core form pads every block to 128 x 128 x 32
-  // tiles; it is used when at least 30% of the padded work is useful (the
-  // small MPO contractions, with k and n of a few units, stay on the FP64
-  // kernel where they are memory-bound anyway).
-  if (prec == kTF32x3) {
-    double useful = 0.0, padded = 0.0;
+  // Small B (an MPO tensor): the tall-skinny kernel reads A in place.
+  if (b.size() <= 65536) {
+    int64_t max_k = 0, max_n = 0;
     for (auto &kv : out) {
-      int64_t m = 1, n = 1;
-      for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
+      int64_t n = 1;
       for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
+      max_n = std::max(max_n, n);
+      for (auto &cp : kv.second) {
+        int64_t k = 1;
+        for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
+        max_k = std::max(max_k, k);
+      }
+    }
+    if (skinny_eligible(b, max_k, max_n)) {
+      auto strides = [](const Tensor &t, int64_t blk, int64_t *str) {
+        int64_t s = 1;
+        for (int l = t.rank() - 1; l >= 0; --l) {
+          str[l] = s;
+          s *= t.block_dim(blk, l);
+        }
+      };
+      std::vector<SkinnyPair> sp;
+      std::vector<SkinnyItem> items;
+      std::vector<char> touched(o.nblocks(), 0);
+      const int rows = skinny_rows_per_cta();
+      auto add_items = [&](int64_t c_off, int64_t m, int64_t n, int pb, int pe) {
+        for (int64_t r0 = 0; r0 < m; r0 += rows)
+          items.push_back({c_off, (int)m, (int)n, (int)r0, pb, pe});
+      };
+      for (auto &kv : out) {
+        const int64_t ob = o.find(kv.first.data());
+        GQ_CHECK(ob >= 0, "contraction produces a block missing from the target structure");
+        touched[ob] = 1;
+        int64_t m = 1, n = 1;
+        for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
+        for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
+        const int pb = (int)sp.size();
+        for (auto &cp : kv.second) {
+          int64_t sa[kMaxRank], sb[kMaxRank];
+          strides(a, cp.ablk, sa);
+          strides(b, cp.bblk, sb);
+          SkinnyPair q{};
+          q.a_off = a.offs[cp.ablk];
+          q.b_off = b.offs[cp.bblk];
+          q.nk = nc;
+          q.K = 1;
+          for (int t = 0; t < nc; ++t) {
+            q.k_dims[t] = (int)a.block_dim(cp.ablk, axes_a[t]);
+            q.ka_str[t] = sa[axes_a[t]];
+            q.kb_str[t] = sb[axes_b[t]];
+            q.K *= q.k_dims[t];
+          }
+          q.nfa = (int)free_a.size();
+          for (size_t t = 0; t < free_a.size(); ++t) {
+            q.fa_dims[t] = (int)a.block_dim(cp.ablk, free_a[t]);
+            q.fa_str[t] = sa[free_a[t]];
+          }
+          q.nfb = (int)free_b.size();
+          for (size_t t = 0; t < free_b.size(); ++t) {
+            q.fb_dims[t] = (int)b.block_dim(cp.bblk, free_b[t]);
+            q.fb_str[t] = sb[free_b[t]];
+          }
+          sp.push_back(q);
+          plan->flops += 2.0 * (double)m * (double)n * (double)q.K;
+        }
+        add_items(o.offs[ob], m, n, pb, (int)sp.size());
+      }
+      for (int64_t ob = 0; ob < o.nblocks(); ++ob) {
+        if (touched[ob]) continue;
+        const int *c = o.block_coords(ob);
+        int64_t m = 1, n = 1;
+        for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[c[l]];
+        for (size_t l = nfa; l < o.idx.size(); ++l) n *= o.idx[l].dim[c[l]];
+        add_items(o.offs[ob], m, n, 0, 0);
+        plan->nzero_blocks++;
+      }
+      plan->use_skinny = true;
+      plan->sk_jb = max_n <= 8 ? 8 : (max_n <= 16 ? 16 : 32);
+      plan->sk_nitems = (int64_t)items.size();
+      plan->sk_items.upload(items);
+      plan->sk_pairs.upload(sp);
+      plan->a_elems = a.size();
+      plan->b_elems = b.size();
+      return plan;
+    }
+  }
+
+  // Per output block kernel choice.  The tensor-core form pads every block
+  // to 128 x 128 x 32 tiles; its TF32 rate is a few hundred times this
+  // part's FP64 rate, so a block goes to it when at least 2% of its padded
+  // work is useful.  Tiny blocks and the MPO contractions (k and n of a few
+  // units) stay on the FP64 kernel, where they are memory-bound anyway.
+  struct OutBlock { int64_t ob, m, n; const std::vector<Contrib> *pairs; bool tc; };
+  std::vector<OutBlock> obs;
+  obs.reserve(out.size());
+  std::vector<char> touched(o.nblocks(), 0);
+  bool any_tc = false, any_fp = false;
+  for (auto &kv : out) {
+    const int64_t ob = o.find(kv.first.data());
+    GQ_CHECK(ob >= 0, "contraction produces a block missing from the target structure");
+    touched[ob] = 1;
+    int64_t m = 1, n = 1;
+    for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
+    for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
+    bool tc = false;
+    if (prec == kTF32x3) {
+      double useful = 0.0, padded = 0.0;
       for (auto &cp : kv.second) {
         int64_t k = 1;
         for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
@@ -186,14 +283,23 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
         padded += 2.0 * ((m + 127) / 128 * 128.0) * ((n + 127) / 128 * 128.0) *
                   ((k + 31) / 32 * 32.0);
       }
+      tc = useful >= 0.02 * padded;
+      if (tc) plan->padded_flops += padded;
     }
-    plan->use_tc = padded > 0.0 && useful >= 0.3 * padded;
-    plan->padded_flops = padded;
+    any_tc |= tc;
+    any_fp |= !tc;
+    obs.push_back({ob, m, n, &kv.second, tc});
   }
-  if (plan->use_tc) {
+  // target blocks without contributions are written as zeros by FP64 tiles
+  for (int64_t ob = 0; ob < o.nblocks(); ++ob)
+    if (!touched[ob]) { any_fp = true; plan->nzero_blocks++; }
+
+  plan->use_tc = any_tc;
+  if (any_tc) {
     build_tc_pack(a, free_a, axes_a, plan->ta);
     build_tc_pack(b, free_b, axes_b, plan->tb);
-  } else {
+  }
+  if (any_fp) {
     if (is_identity(pa)) {
       plan->transA = 0;
     } else if (is_identity(pa_t)) {
@@ -212,40 +318,14 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
     }
   }
 
-  const Precision kern = plan->use_tc ? kTF32x3 : kFP64;
-  const int TM = gemm_tile_m(kern), TN = gemm_tile_n(kern);
-  plan->tile_m = TM;
-  plan->tile_n = TN;
-  std::vector<GemmTile> tiles;
-  std::vector<GemmPair> pairs;
-  std::vector<char> touched(o.nblocks(), 0);
-  for (auto &kv : out) {
-    const int64_t ob = o.find(kv.first.data());
-    GQ_CHECK(ob >= 0, "contraction produces a block missing from the target structure");
-    touched[ob] = 1;
-    int64_t m = 1, n = 1;
-    for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
-    for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
-    const int pbeg = (int)pairs.size();
-    int64_t ksum = 0;
-    for (auto &cp : kv.second) {
-      int64_t k = 1;
-      for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
-      GemmPair gp{};
-      gp.a_off = plan->use_tc ? plan->ta.base[cp.ablk] : a.offs[cp.ablk];
-      gp.b_off = plan->use_tc ? plan->tb.base[cp.bblk] : b.offs[cp.bblk];
-      gp.k = (int)k;
-      gp.lda = (int)(plan->transA ? m : k);
-      gp.ldb = (int)(plan->transB ? k : n);
-      pairs.push_back(gp);
-      ksum += k;
-      plan->flops += 2.0 * (double)m * (double)n * (double)k;
-    }
-    const int pend = (int)pairs.size();
+  std::vector<GemmTile> tiles, tiles_tc;
+  std::vector<GemmPair> pairs, pairs_tc;
+  auto add_tiles = [](std::vector<GemmTile> &dst, int64_t c_off, int64_t m, int64_t n, int pbeg,
+                      int pend, int64_t ksum, int TM, int TN) {
     for (int64_t r0 = 0; r0 < m; r0 += TM)
       for (int64_t c0 = 0; c0 < n; c0 += TN) {
         GemmTile t{};
-        t.c_off = o.offs[ob];
+        t.c_off = c_off;
         t.m = (int)m;
         t.n = (int)n;
         t.row0 = (int)r0;
@@ -253,36 +333,55 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
         t.pair_begin = pbeg;
         t.pair_end = pend;
         t.work = ksum * std::min<int64_t>(TM, m - r0) * std::min<int64_t>(TN, n - c0);
-        tiles.push_back(t);
+        dst.push_back(t);
       }
+  };
+  for (auto &b0 : obs) {
+    auto &pl = b0.tc ? pairs_tc : pairs;
+    const int pbeg = (int)pl.size();
+    int64_t ksum = 0;
+    for (auto &cp : *b0.pairs) {
+      int64_t k = 1;
+      for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
+      GemmPair gp{};
+      gp.a_off = b0.tc ? plan->ta.base[cp.ablk] : a.offs[cp.ablk];
+      gp.b_off = b0.tc ? plan->tb.base[cp.bblk] : b.offs[cp.bblk];
+      gp.k = (int)k;
+      gp.lda = (int)(plan->transA ? b0.m : k);
+      gp.ldb = (int)(plan->transB ? k : b0.n);
+      pl.push_back(gp);
+      ksum += k;
+      const double f = 2.0 * (double)b0.m * (double)b0.n * (double)k;
+      plan->flops += f;
+      if (b0.tc) plan->flops_tc += f;
+    }
+    if (b0.tc)
+      add_tiles(tiles_tc, o.offs[b0.ob], b0.m, b0.n, pbeg, (int)pl.size(), ksum,
+                gemm_tile_m(kTF32x3), gemm_tile_n(kTF32x3));
+    else
+      add_tiles(tiles, o.offs[b0.ob], b0.m, b0.n, pbeg, (int)pl.size(), ksum,
+                gemm_tile_m(kFP64), gemm_tile_n(kFP64));
   }
-  // Target blocks without contributions are written as zeros by empty tiles.
   for (int64_t ob = 0; ob < o.nblocks(); ++ob) {
     if (touched[ob]) continue;
     const int *c = o.block_coords(ob);
     int64_t m = 1, n = 1;
     for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[c[l]];
     for (size_t l = nfa; l < o.idx.size(); ++l) n *= o.idx[l].dim[c[l]];
-    for (int64_t r0 = 0; r0 < m; r0 += TM)
-      for (int64_t c0 = 0; c0 < n; c0 += TN) {
-        GemmTile t{};
-        t.c_off = o.offs[ob];
-        t.m = (int)m;
-        t.n = (int)n;
-        t.row0 = (int)r0;
-        t.col0 = (int)c0;
-        t.pair_begin = t.pair_end = 0;
-        t.work = 0;
-        tiles.push_back(t);
-      }
-    plan->nzero_blocks++;
+    add_tiles(tiles, o.offs[ob], m, n, 0, 0, 0, gemm_tile_m(kFP64), gemm_tile_n(kFP64));
   }
-  // Longest tiles first so the tail of the grid is short ones.
-  std::stable_sort(tiles.begin(), tiles.end(),
-                   [](const GemmTile &x, const GemmTile &y) { return x.work > y.work; });
+  // Longest tiles first so the tail of each grid is short ones.
+  auto by_work = [](const GemmTile &x, const GemmTile &y) { return x.work > y.work; };
+  std::stable_sort(tiles.begin(), tiles.end(), by_work);
+  std::stable_sort(tiles_tc.begin(), tiles_tc.end(), by_work);
+  plan->tile_m = gemm_tile_m(any_tc ? kTF32x3 : kFP64);
+  plan->tile_n = gemm_tile_n(any_tc ? kTF32x3 : kFP64);
   plan->ntiles = (int64_t)tiles.size();
   plan->tiles.upload(tiles);
   plan->pairs.upload(pairs);
+  plan->ntiles_tc = (int64_t)tiles_tc.size();
+  plan->tiles_tc.upload(tiles_tc);
+  plan->pairs_tc.upload(pairs_tc);
   plan->a_elems = a.size();
   plan->b_elems = b.size();
   return plan;
@@ -296,14 +395,16 @@ float *align16(double *p) {
 }  // namespace
 
 int64_t contract_scratch(const ContractPlan &p) {
+  if (p.use_skinny) return 0;
+  int64_t s = (p.pa.needed ? p.pa.total : 0) + (p.pb.needed ? p.pb.total : 0);
   if (p.use_tc)
-    return (p.a_cached ? 0 : floats_as_doubles(p.ta.floats)) +
-           (p.b_cached ? 0 : floats_as_doubles(p.tb.floats));
-  return (p.pa.needed ? p.pa.total : 0) + (p.pb.needed ? p.pb.total : 0);
+    s += (p.a_cached ? 0 : floats_as_doubles(p.ta.floats)) +
+         (p.b_cached ? 0 : floats_as_doubles(p.tb.floats));
+  return s;
 }
 
 void cache_operand(ContractPlan &p, int which, const double *src) {
-  if (!p.use_tc) return;
+  if (!p.use_tc || p.use_skinny) return;
   if (which == 0) {
     p.a_packed.alloc(floats_as_doubles(p.ta.floats));
     run_tc_pack(p.ta, src, align16(p.a_packed.p));
@@ -317,8 +418,12 @@ void cache_operand(ContractPlan &p, int which, const double *src) {
 
 void run_contract(const ContractPlan &p, const double *a, const double *b, double *c,
                   double *scratch, Precision) {
-  if (p.use_tc) {
-    double *s = scratch;
+  if (p.use_skinny) {
+    launch_skinny(p, a, b, c);
+    return;
+  }
+  double *s = scratch;
+  if (p.use_tc && p.ntiles_tc > 0) {
     const float *A, *B;
     if (p.a_cached) {
       A = align16(p.a_packed.p);
@@ -332,12 +437,12 @@ void run_contract(const ContractPlan &p, const double *a, const double *b, doubl
     } else {
       run_tc_pack(p.tb, b, align16(s));
       B = align16(s);
+      s += floats_as_doubles(p.tb.floats);
     }
-    if (p.ntiles > 0) launch_gemm_tf32x3(p, A, B, c);
-    return;
+    launch_gemm_tf32x3(p, A, B, c);
   }
+  if (p.ntiles == 0) return;
   const double *A = a, *B = b;
-  double *s = scratch;
   if (p.pa.needed) {
     run_perm(p.pa, a, s);
     A = s;
@@ -347,7 +452,6 @@ void run_contract(const ContractPlan &p, const double *a, const double *b, doubl
     run_perm(p.pb, b, s);
     B = s;
   }
-  if (p.ntiles == 0) return;
   launch_gemm_fp64(p, A, B, c);
 }
 
@@ -466,7 +570,7 @@ void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, d
   else
     gemm_fp64_kernel<1, 1><<<grid, 256, 0, s>>>(p.tiles.p, p.pairs.p, A, B, C);
   GQ_CUDA(cudaGetLastError());
-  prof_end(kProfGemmFp64, p.flops, 8.0 * (double)(p.a_elems + p.b_elems));
+  prof_end(kProfGemmFp64, p.flops - p.flops_tc, 8.0 * (double)(p.a_elems + p.b_elems));
 }
 
 }  // namespace gq

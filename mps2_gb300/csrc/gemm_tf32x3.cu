@@ -521,10 +521,10 @@ void launch_gemm_tf32x3(const ContractPlan &p, const float *A, const float *B, d
   }
   int *err = reinterpret_cast<int *>(ctx().dev_scalars + 63);
   prof_begin(kProfGemmTf32);
-  gemm_tf32x3_kernel<<<(unsigned)p.ntiles, tc::kThreads, smem, stream()>>>(p.tiles.p, p.pairs.p, A,
-                                                                           B, C, err);
+  gemm_tf32x3_kernel<<<(unsigned)p.ntiles_tc, tc::kThreads, smem, stream()>>>(
+      p.tiles_tc.p, p.pairs_tc.p, A, B, C, err);
   GQ_CUDA(cudaGetLastError());
-  prof_end(kProfGemmTf32, p.flops, 8.0 * (double)(p.a_elems + p.b_elems));
+  prof_end(kProfGemmTf32, p.flops_tc, 8.0 * (double)(p.a_elems + p.b_elems));
 }
 
 int *tc_error_flag() { return reinterpret_cast<int *>(ctx().dev_scalars + 63); }

@@ -76,6 +76,21 @@ struct PermPlan {
   int64_t nchunks = 0;
 };
 
+// Tall-skinny contraction with a small (MPO) B operand: one pair of blocks
+// read in place through leg strides (skinny.cu).
+constexpr int kSkMaxK = 64;
+struct SkinnyPair {
+  int64_t a_off, b_off;
+  int K, nk, nfa, nfb;
+  int k_dims[kMaxRank];
+  int64_t ka_str[kMaxRank], kb_str[kMaxRank];
+  int fa_dims[kMaxRank];
+  int64_t fa_str[kMaxRank];
+  int fb_dims[kMaxRank];
+  int64_t fb_str[kMaxRank];
+};
+struct SkinnyItem { int64_t c_off; int M, N, row0, pair_begin, pair_end; };
+
 // Packed split-precision operand: every block as 128-row x 32-k tiles of
 // TF32 hi then lo, each tile in the tensor-core shared-memory image.
 struct TcPackPlan {
@@ -89,14 +104,23 @@ struct ContractPlan {
   TensorPtr out;          // output structure (no data)
   int transA = 0, transB = 0;
   PermPlan pa, pb;
+  bool use_skinny = false;  // small-B tall-skinny kernel (skinny.cu)
+  DevArray<SkinnyItem> sk_items;
+  DevArray<SkinnyPair> sk_pairs;
+  int64_t sk_nitems = 0;
+  int sk_jb = 8;
   bool use_tc = false;    // 3xTF32 tcgen05 kernel (else the FP64 kernel)
   TcPackPlan ta, tb;
   bool a_cached = false, b_cached = false;  // constant operand packed once
   DevBuf a_packed, b_packed;
   double padded_flops = 0.0;
-  DevArray<GemmTile> tiles;
+  DevArray<GemmTile> tiles;       // FP64-kernel tiles (and zero blocks)
   DevArray<GemmPair> pairs;
   int64_t ntiles = 0;
+  DevArray<GemmTile> tiles_tc;    // tensor-core tiles (128 x 128)
+  DevArray<GemmPair> pairs_tc;    // offsets into the packed operands
+  int64_t ntiles_tc = 0;
+  double flops_tc = 0.0;
   int64_t nzero_blocks = 0;   // output blocks with no contribution
   DevArray<int64_t> zero_blocks;  // (offset, size) pairs to clear
   double flops = 0.0;         // 2*m*n*k summed over block products
@@ -121,6 +145,11 @@ TensorPtr contract(const Tensor &a, const Tensor &b, const std::vector<int> &axe
 // Pack a constant operand of the plan once (which = 0: A, 1: B); later
 // run_contract calls ignore that operand's pointer.
 void cache_operand(ContractPlan &p, int which, const double *src);
+
+// Tall-skinny kernel (launched by run_contract when use_skinny).
+bool skinny_eligible(const Tensor &b, int64_t max_k, int64_t max_n);
+void launch_skinny(const ContractPlan &p, const double *A, const double *B, double *C);
+int skinny_rows_per_cta();
 
 // GEMM kernels (launched by run_contract)
 void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, double *C);
@@ -203,6 +232,9 @@ double matvec_flops(const MatvecPlan &p);
 struct LanczosParamsC {
   double error = 1e-7;
   int64_t max_iterations = 200;
+  // Split form only: recompute the reported energy as the FP64 Rayleigh
+  // quotient <gs|H|gs>/<gs|gs> with one FP64 matvec.
+  bool fp64_rayleigh = true;
 };
 struct LanczosResult {
   int64_t iters = 0;
@@ -211,6 +243,7 @@ struct LanczosResult {
   int64_t matvecs = 0;
   double matvec_flops = 0.0;
   double matvec_seconds = 0.0;
+  double ritz_energy = 0.0;   // the Lanczos (Ritz) value before any correction
 };
 // The Lanczos space: every block allowed by the state's legs and div.
 TensorPtr lanczos_space(const Tensor &state);

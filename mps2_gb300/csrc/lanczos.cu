@@ -212,7 +212,21 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
     dev_combine(ptrs, c, gs->data.p, n);
     res.iters = iters;
     res.energy = energy;
+    res.ritz_energy = energy;
     res.gs = gs;
+    if (prec == kTF32x3 && prm.fp64_rayleigh) {
+      // FP64 Rayleigh quotient of the split-precision ground state
+      auto p64 = plan_matvec(h, init, kFP64);
+      run_matvec(*p64, gs->data.p, last.p);
+      dev_dot(gs->data.p, last.p, n, a_dev, red.p);
+      dev_dot(gs->data.p, gs->data.p, n, n_dev, red.p);
+      GQ_CUDA(cudaMemcpyAsync(hs, a_dev, sizeof(double), cudaMemcpyDeviceToHost, stream()));
+      GQ_CUDA(cudaMemcpyAsync(hs + 1, n_dev, sizeof(double), cudaMemcpyDeviceToHost, stream()));
+      sync();
+      res.energy = hs[0] / hs[1];
+      res.matvecs++;
+      res.matvec_flops += p64->flops;
+    }
   };
 
   int64_t m = 0;

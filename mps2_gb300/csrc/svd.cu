@@ -8,17 +8,30 @@
 //    q = ldiv - sum_{l<ldims} dir_l q_l form one dense matrix (rows: row-leg
 //    sector tuples ascending, columns likewise; every allowed block takes
 //    part, absent ones are zero);
-//  * every group is decomposed in FP64 (cuSOLVER gesvdj, sorted);
-//  * values <= 1e-13 * s_max become exact zeros;
+//  * each group has min(m, n) singular values; values <= 1e-13 * s_max
+//    (global) are exact zeros;
 //  * global selection: rank all values (ties: earlier group, earlier
 //    position); D = smallest count in [Dmin, Dmax] whose discarded weight
 //    sum_{i>=D} s_i^2 / sum s^2 <= trunc_err, capped by Dmax and #values;
-//  * kept nonzero values use the solver's vectors with the largest-|.|
-//    entry of each left vector made positive (right vector follows); kept
-//    zero values use the canonical completion of null_completion (a
-//    counter-hashed seed matrix projected off the group's nonzero singular
-//    vectors, then CholeskyQR2);
+//  * kept nonzero values: the largest-|.| entry of each left vector is made
+//    positive (the right vector follows); kept zero values use the
+//    canonical completion of null_completion (a counter-hashed seed matrix
+//    projected off the group's nonzero singular vectors, then CholeskyQR2);
 //  * new bond sectors: groups with a kept value, ascending charge.
+//
+// Decomposition routes (all FP64):
+//  * groups with m, n <= 32: one batched Jacobi SVD for all of them;
+//  * larger groups inside a sweep update: only the factor that becomes the
+//    canonical MPS tensor has to be orthonormal, so it is taken from the
+//    eigenvectors of the Gram matrix on that side (syevd) and the other
+//    factor comes by projection without dividing by singular values --
+//    'r' updates: U from Theta Theta^T and S.Vt = U^T Theta; 'l' updates:
+//    V from Theta^T Theta and U.S = Theta V.  The Gram matrices are solved
+//    in size buckets with one batched eigensolve per bucket.  On these
+//    groups eigenvalues below 1e-14 of the group's largest are the
+//    eigensolver's noise floor and count as exact zeros (singular values
+//    below ~1e-7 of the group's largest);
+//  * larger groups of a plain SVD (both factors orthonormal): Jacobi SVD.
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
@@ -31,11 +44,23 @@ namespace gq {
 
 namespace {
 constexpr double kZeroSvRtol = 1e-13;
+constexpr double kGramZeroRtol = 1e-14;
+constexpr int kSmall = 32;
+
+enum Route { kSmallJacobi = 0, kJacobi = 1, kGramLeft = 2, kGramRight = 3 };
 
 #define GQ_SOLVER(call)                                                               \
   do {                                                                                \
     cusolverStatus_t s_ = (call);                                                     \
     if (s_ != CUSOLVER_STATUS_SUCCESS)                                                \
+      ::gq::fail(::gq::kSolverError, std::string(#call) + " failed with status " +    \
+                                         std::to_string((int)s_));                    \
+  } while (0)
+
+#define GQ_BLAS(call)                                                                 \
+  do {                                                                                \
+    cublasStatus_t s_ = (call);                                                       \
+    if (s_ != CUBLAS_STATUS_SUCCESS)                                                  \
       ::gq::fail(::gq::kSolverError, std::string(#call) + " failed with status " +    \
                                          std::to_string((int)s_));                    \
   } while (0)
@@ -52,6 +77,16 @@ cusolverDnHandle_t solver() {
   return h;
 }
 
+cublasHandle_t blas() {
+  static cublasHandle_t h = nullptr;
+  if (!h) GQ_BLAS(cublasCreate(&h));
+  GQ_BLAS(cublasSetStream(h, stream()));
+  return h;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
 struct GatherItem { int64_t src_off, dst_off; int rows, cols, ld; };
 
 __global__ void gather_kernel(const GatherItem *__restrict__ items, const double *__restrict__ src,
@@ -64,8 +99,45 @@ __global__ void gather_kernel(const GatherItem *__restrict__ items, const double
   }
 }
 
-// Sign convention: column j of `u` (m x *, col-major, ld m): make the first
-// entry of largest magnitude positive; flip column j of `v` alongside.
+// A group matrix X (col-major n x m, ld n) into a zero-padded 32 x 32 slot.
+struct PadItem { int64_t src_off, dst_off; int n, m; };
+
+__global__ void pad_small_kernel(const PadItem *__restrict__ items, const double *__restrict__ src,
+                                 double *__restrict__ dst) {
+  const PadItem it = items[blockIdx.x];
+  for (int e = threadIdx.x; e < kSmall * kSmall; e += blockDim.x) {
+    const int r = e % kSmall, c = e / kSmall;
+    dst[it.dst_off + e] = (r < it.n && c < it.m) ? src[it.src_off + r + (int64_t)c * it.n] : 0.0;
+  }
+}
+
+// Gram slot set-up: outside the leading dim x dim block, -1 on the diagonal
+// and 0 elsewhere (the leading block is written by the Gram GEMM).
+struct PadDiagItem { int64_t off; int bs, dim; };
+
+__global__ void pad_diag_kernel(const PadDiagItem *__restrict__ items, double *__restrict__ buf) {
+  const PadDiagItem it = items[blockIdx.x];
+  const int64_t n = (int64_t)it.bs * it.bs;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const int r = (int)(e % it.bs), c = (int)(e / it.bs);
+    if (r >= it.dim || c >= it.dim) buf[it.off + e] = (r == c) ? -1.0 : 0.0;
+  }
+}
+
+// Column copies: dst[:, dcol] = src[:, scol] * scale over `rows` rows.
+struct ColItem { int64_t src_off, dst_off; int rows, ld_src, ld_dst, scol, dcol; double scale; };
+
+__global__ void col_copy_kernel(const ColItem *__restrict__ items, const double *__restrict__ src,
+                                double *__restrict__ dst) {
+  const ColItem it = items[blockIdx.x];
+  const double *s = src + it.src_off + (int64_t)it.scol * it.ld_src;
+  double *d = dst + it.dst_off + (int64_t)it.dcol * it.ld_dst;
+  for (int r = threadIdx.x; r < it.rows; r += blockDim.x) d[r] = s[r] * it.scale;
+}
+
+// Sign convention: column of `u` (m entries): make the first entry of
+// largest magnitude positive; flip the matching column of `v` (n entries)
+// alongside.
 struct SignItem { int64_t u_off, v_off; int m, n; };
 
 __global__ void sign_fix_kernel(const SignItem *__restrict__ items, double *__restrict__ U,
@@ -100,39 +172,23 @@ __global__ void sign_fix_kernel(const SignItem *__restrict__ items, double *__re
   for (int i = threadIdx.x; i < it.n; i += blockDim.x) V[it.v_off + i] = -V[it.v_off + i];
 }
 
-// Output block writer.  mode 0: U block (rows x k, row-major) with
-// dst(i,j) = col j of the group's left vectors at row `r0 + i`;
-// mode 1: Vt block (k x rows) with dst(j,i) = col j of the right vectors at
-// row `r0 + i`.  Columns j < knz come from the SVD, j >= knz from the
-// completion.  `scale` multiplies column j by s[j] when set.
-struct ScatterItem {
-  int64_t dst_off;
-  int rows, k, knz, mode, scale;
-  int64_t svd_off; int ld_svd;      // col-major vectors, row offset folded in
-  int64_t comp_off; int ld_comp;
-  int64_t s_off;
-};
+// Output blocks.  mode 0: U block (rows x k, row-major), element (i, j) =
+// L[r0 + i, j]; mode 1: Vt block (k x rows), element (j, i) = R[r0 + i, j];
+// L and R are the group's col-major factors (ld = group m or n).
+struct ScatterItem { int64_t dst_off, src_off; int rows, k, ld, mode; };
 
-__global__ void scatter_kernel(const ScatterItem *__restrict__ items,
-                               const double *__restrict__ left_svd,
-                               const double *__restrict__ right_svd,
-                               const double *__restrict__ left_comp,
-                               const double *__restrict__ right_comp,
-                               const double *__restrict__ svals, double *__restrict__ U,
+__global__ void scatter_kernel(const ScatterItem *__restrict__ items, const double *__restrict__ L,
+                               const double *__restrict__ R, double *__restrict__ U,
                                double *__restrict__ Vt) {
   const ScatterItem it = items[blockIdx.x];
-  const double *svd = it.mode == 0 ? left_svd : right_svd;
-  const double *comp = it.mode == 0 ? left_comp : right_comp;
+  const double *src = it.mode == 0 ? L : R;
   double *dst = it.mode == 0 ? U : Vt;
   const int64_t n = (int64_t)it.rows * it.k;
   for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
     int i, j;
     if (it.mode == 0) { i = (int)(e / it.k); j = (int)(e % it.k); }
     else { j = (int)(e / it.rows); i = (int)(e % it.rows); }
-    double v = j < it.knz ? svd[it.svd_off + i + (int64_t)j * it.ld_svd]
-                          : comp[it.comp_off + i + (int64_t)(j - it.knz) * it.ld_comp];
-    if (it.scale) v *= svals[it.s_off + j];
-    dst[it.dst_off + e] = v;
+    dst[it.dst_off + e] = src[it.src_off + i + (int64_t)j * it.ld];
   }
 }
 
@@ -157,37 +213,20 @@ __global__ void seed_matrix_kernel(double *__restrict__ w, int dim, int k,
   }
 }
 
-#define GQ_BLAS(call)                                                                 \
-  do {                                                                                \
-    cublasStatus_t s_ = (call);                                                       \
-    if (s_ != CUBLAS_STATUS_SUCCESS)                                                  \
-      ::gq::fail(::gq::kSolverError, std::string(#call) + " failed with status " +    \
-                                         std::to_string((int)s_));                    \
-  } while (0)
-
-cublasHandle_t blas() {
-  static cublasHandle_t h = nullptr;
-  if (!h) GQ_BLAS(cublasCreate(&h));
-  GQ_BLAS(cublasSetStream(h, stream()));
-  return h;
+template <typename T>
+void launch_items(void (*kern)(const T *, const double *, double *), const std::vector<T> &items,
+                  const double *src, double *dst) {
+  if (items.empty()) return;
+  DevArray<T> d;
+  d.upload(items);
+  kern<<<(unsigned)items.size(), 256, 0, stream()>>>(d.p, src, dst);
+  GQ_CUDA(cudaGetLastError());
 }
-
-struct Group {
-  QN q;
-  std::vector<std::vector<int>> rows, cols;
-  std::vector<int64_t> rsz, csz, roff, coff;
-  int64_t m = 0, n = 0, p = 0;
-  int64_t mat_off = 0, lv_off = 0, rv_off = 0, s_off = 0;  // in the work buffers
-  int64_t nnz = 0;     // nonzero singular values
-  int64_t keep = 0, keep_nz = 0;
-  int sector = -1;
-  int64_t lc_off = 0, rc_off = 0;  // completion buffers
-};
 
 // Canonical completion: k orthonormal columns orthogonal to the r
 // orthonormal columns of `vecs` (dim x r, col-major, ld dim), written to
-// out (dim x k, col-major).  The seed matrix is projected off `vecs` twice
-// (Gram-Schmidt with re-orthogonalisation) and orthonormalised by
+// out (dim x k, col-major, ld dim).  The seed matrix is projected off `vecs`
+// twice (Gram-Schmidt with re-orthogonalisation) and orthonormalised by
 // CholeskyQR2; nothing depends on the signs of the columns of `vecs`.
 void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, int group, int side,
                      double *out) {
@@ -230,6 +269,26 @@ void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, int 
   if (hinfo[0] != 0 || hinfo[1] != 0)
     fail(kSolverError, "null-space completion: Cholesky failed");
 }
+
+struct Group {
+  QN q;
+  std::vector<std::vector<int>> rows, cols;
+  std::vector<int64_t> rsz, csz, roff, coff;
+  int64_t m = 0, n = 0, p = 0;
+  Route route = kJacobi;
+  int64_t mat_off = 0;            // row-major m x n (= col-major X, n x m, ld n)
+  int64_t lv_off = 0, rv_off = 0; // left (m rows) / right (n rows) singular vectors
+  int ld_l = 0, ld_r = 0;
+  int64_t sv_off = 0;             // singular values (small: 32 per group, jacobi: p)
+  int64_t ev_off = 0, w_off = 0;  // gram: eigenvectors (dim x dim) and eigenvalues
+  int64_t dim = 0;
+  int64_t small_idx = -1;
+  std::vector<double> svals;      // p values, descending
+  std::vector<int> src_cols;      // source column of each value
+  int64_t nnz = 0, keep = 0, keep_nz = 0;
+  int sector = -1;
+  int64_t L_off = 0, R_off = 0;   // outputs: L (m x keep), R (n x keep)
+};
 }  // namespace
 
 SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_err,
@@ -263,7 +322,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     brefs.push_back(std::move(br));
   }
   std::vector<Group *> groups;
-  int64_t mat_total = 0, lv_total = 0, rv_total = 0, s_total = 0;
+  int64_t mat_total = 0, n_small = 0;
   for (auto &kv : gmap) {
     Group &g = kv.second;
     std::sort(g.rows.begin(), g.rows.end());
@@ -287,12 +346,16 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     g.p = std::min(g.m, g.n);
     g.mat_off = mat_total;
     mat_total += g.m * g.n;
-    g.lv_off = lv_total;
-    lv_total += g.m * g.p;
-    g.rv_off = rv_total;
-    rv_total += g.n * g.p;
-    g.s_off = s_total;
-    s_total += g.p;
+    if (g.m <= kSmall && g.n <= kSmall) {
+      g.route = kSmallJacobi;
+      g.small_idx = n_small++;
+    } else if (scale_side == 2) {
+      g.route = kGramLeft;
+    } else if (scale_side == 1) {
+      g.route = kGramRight;
+    } else {
+      g.route = kJacobi;
+    }
     groups.push_back(&g);
   }
   GQ_CHECK(!groups.empty(), "SVD of a tensor without blocks");
@@ -306,66 +369,222 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       Group &g = gmap[br.q];
       const int64_t ri = std::lower_bound(g.rows.begin(), g.rows.end(), br.rc) - g.rows.begin();
       const int64_t ci = std::lower_bound(g.cols.begin(), g.cols.end(), br.cc) - g.cols.begin();
-      GatherItem it{};
-      it.src_off = t.offs[br.b];
-      it.dst_off = g.mat_off + g.roff[ri] * g.n + g.coff[ci];
-      it.rows = (int)g.rsz[ri];
-      it.cols = (int)g.csz[ci];
-      it.ld = (int)g.n;
-      items.push_back(it);
+      items.push_back({t.offs[br.b], g.mat_off + g.roff[ri] * g.n + g.coff[ci], (int)g.rsz[ri],
+                       (int)g.csz[ci], (int)g.n});
     }
-    DevArray<GatherItem> d;
-    d.upload(items);
-    gather_kernel<<<(unsigned)items.size(), 256, 0, s>>>(d.p, t.data.p, mats.p);
-    GQ_CUDA(cudaGetLastError());
+    launch_items(gather_kernel, items, t.data.p, mats.p);
   }
 
-  // ---- per-group SVD (the row-major m x n matrix is col-major n x m) -------
-  DevBuf lv(lv_total), rv(rv_total), sv(s_total);
-  {
-    auto h = solver();
-    gesvdjInfo_t prm;
-    GQ_SOLVER(cusolverDnCreateGesvdjInfo(&prm));
+  // ---- decompositions -----------------------------------------------------
+  auto h = solver();
+  auto bh = blas();
+  gesvdjInfo_t prm;
+  GQ_SOLVER(cusolverDnCreateGesvdjInfo(&prm));
+  // small groups: one batched Jacobi SVD on zero-padded 32 x 32 slots of X
+  const int64_t slot = kSmall * kSmall;
+  DevBuf sbatch(n_small * slot), su(n_small * slot), sv(n_small * slot), ss(n_small * kSmall);
+  DevArray<int> sinfo;
+  if (n_small > 0) {
+    std::vector<PadItem> items;
+    for (Group *g : groups)
+      if (g->route == kSmallJacobi)
+        items.push_back({g->mat_off, g->small_idx * slot, (int)g->n, (int)g->m});
+    launch_items(pad_small_kernel, items, mats.p, sbatch.p);
+    int lw = 0;
+    GQ_SOLVER(cusolverDnDgesvdjBatched_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, kSmall, kSmall,
+                                                  sbatch.p, kSmall, ss.p, su.p, kSmall, sv.p,
+                                                  kSmall, &lw, prm, (int)n_small));
+    DevBuf work((int64_t)lw + 1);
+    sinfo.upload(std::vector<int>(n_small, 0));
+    GQ_SOLVER(cusolverDnDgesvdjBatched(h, CUSOLVER_EIG_MODE_VECTOR, kSmall, kSmall, sbatch.p,
+                                       kSmall, ss.p, su.p, kSmall, sv.p, kSmall, work.p, lw,
+                                       sinfo.p, prm, (int)n_small));
+    // X = Ux S Vx^T with X = Theta^T: Theta's left vectors are Vx (sv),
+    // its right vectors Ux (su)
+    for (Group *g : groups)
+      if (g->route == kSmallJacobi) {
+        g->lv_off = g->rv_off = g->small_idx * slot;
+        g->ld_l = g->ld_r = kSmall;
+        g->sv_off = g->small_idx * kSmall;
+      }
+  }
+  // larger groups of a plain SVD: Jacobi SVD each (sorted)
+  int64_t jl_total = 0, jr_total = 0, js_total = 0;
+  for (Group *g : groups)
+    if (g->route == kJacobi) {
+      g->lv_off = jl_total;
+      jl_total += g->m * g->p;
+      g->rv_off = jr_total;
+      jr_total += g->n * g->p;
+      g->sv_off = js_total;
+      js_total += g->p;
+      g->ld_l = (int)g->m;
+      g->ld_r = (int)g->n;
+    }
+  DevBuf jl(jl_total), jr(jr_total), js(js_total);
+  DevArray<int> jinfo;
+  if (js_total > 0) {
     GQ_SOLVER(cusolverDnXgesvdjSetSortEig(prm, 1));
     int lwork = 0;
     for (Group *g : groups) {
+      if (g->route != kJacobi) continue;
       int lw = 0;
-      // X = Theta^T (n x m col-major); X = Ux S Vx^T -> left vectors of
-      // Theta are Vx (m x p), right vectors are Ux (n x p).
       GQ_SOLVER(cusolverDnDgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)g->n, (int)g->m,
-                                             mats.p + g->mat_off, (int)g->n, sv.p + g->s_off,
-                                             rv.p + g->rv_off, (int)g->n, lv.p + g->lv_off,
+                                             mats.p + g->mat_off, (int)g->n, js.p + g->sv_off,
+                                             jr.p + g->rv_off, (int)g->n, jl.p + g->lv_off,
                                              (int)g->m, &lw, prm));
       lwork = std::max(lwork, lw);
     }
     DevBuf work((int64_t)lwork + 1);
-    DevArray<int> infos;
-    infos.upload(std::vector<int>(groups.size(), 0));
+    jinfo.upload(std::vector<int>(groups.size(), 0));
     for (size_t gi = 0; gi < groups.size(); ++gi) {
       Group *g = groups[gi];
+      if (g->route != kJacobi) continue;
       GQ_SOLVER(cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, (int)g->n, (int)g->m,
-                                  mats.p + g->mat_off, (int)g->n, sv.p + g->s_off,
-                                  rv.p + g->rv_off, (int)g->n, lv.p + g->lv_off, (int)g->m, work.p,
-                                  lwork, infos.p + gi, prm));
+                                  mats.p + g->mat_off, (int)g->n, js.p + g->sv_off,
+                                  jr.p + g->rv_off, (int)g->n, jl.p + g->lv_off, (int)g->m, work.p,
+                                  lwork, jinfo.p + gi, prm));
     }
-    std::vector<int> hinfo(groups.size());
-    GQ_CUDA(cudaMemcpyAsync(hinfo.data(), infos.p, sizeof(int) * groups.size(),
+  }
+  // Gram groups: the canonical side's Gram matrix (eigenvalues in [0, |Theta|^2])
+  // in a slot padded to a bucket size with -1 on the extra diagonal, so the
+  // padding's eigenpairs sort below the real ones and stay in the padded
+  // coordinates; one batched eigensolve per bucket.
+  std::map<int64_t, std::vector<Group *>> buckets;
+  for (Group *g : groups)
+    if (g->route == kGramLeft || g->route == kGramRight) {
+      const int64_t real = g->route == kGramLeft ? g->m : g->n;
+      g->dim = real <= 64 ? (real + 31) / 32 * 32 : (real + 63) / 64 * 64;
+      buckets[g->dim].push_back(g);
+    }
+  int64_t ev_total = 0, w_total = 0, n_gram = 0;
+  for (auto &kv : buckets)
+    for (Group *g : kv.second) {
+      g->ev_off = ev_total;
+      ev_total += g->dim * g->dim;
+      g->w_off = w_total;
+      w_total += g->dim;
+      ++n_gram;
+    }
+  DevBuf ev(ev_total), w(w_total);
+  DevArray<int> einfo;
+  if (n_gram > 0) {
+    std::vector<PadDiagItem> pads;
+    for (auto &kv : buckets)
+      for (Group *g : kv.second)
+        pads.push_back({g->ev_off, (int)g->dim, (int)(g->route == kGramLeft ? g->m : g->n)});
+    {
+      DevArray<PadDiagItem> d;
+      d.upload(pads);
+      pad_diag_kernel<<<(unsigned)pads.size(), 256, 0, s>>>(d.p, ev.p);
+      GQ_CUDA(cudaGetLastError());
+    }
+    const double one = 1.0, zero = 0.0;
+    for (auto &kv : buckets)
+      for (Group *g : kv.second) {
+        const int m = (int)g->m, n = (int)g->n, bs = (int)g->dim;
+        const double *X = mats.p + g->mat_off;  // col-major n x m
+        if (g->route == kGramLeft)  // Theta Theta^T = X^T X (m x m)
+          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, X, n, X, n, &zero,
+                              ev.p + g->ev_off, bs));
+        else  // Theta^T Theta = X X^T (n x n)
+          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_T, n, n, m, &one, X, n, X, n, &zero,
+                              ev.p + g->ev_off, bs));
+      }
+    cusolverDnParams_t sp;
+    GQ_SOLVER(cusolverDnCreateParams(&sp));
+    size_t dws = 0, hws = 0;
+    for (auto &kv : buckets) {
+      const int64_t bs = kv.first, nb = (int64_t)kv.second.size();
+      size_t d1 = 0, h1 = 0;
+      GQ_SOLVER(cusolverDnXsyevBatched_bufferSize(
+          h, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, bs, CUDA_R_64F,
+          ev.p + kv.second[0]->ev_off, bs, CUDA_R_64F, w.p + kv.second[0]->w_off, CUDA_R_64F, &d1,
+          &h1, nb));
+      dws = std::max(dws, d1);
+      hws = std::max(hws, h1);
+    }
+    DevBuf dwork((int64_t)(dws / sizeof(double)) + 2);
+    std::vector<char> hwork(hws + 16);
+    einfo.upload(std::vector<int>(n_gram, 0));
+    int64_t io = 0;
+    for (auto &kv : buckets) {
+      const int64_t bs = kv.first, nb = (int64_t)kv.second.size();
+      GQ_SOLVER(cusolverDnXsyevBatched(h, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, bs,
+                                       CUDA_R_64F, ev.p + kv.second[0]->ev_off, bs, CUDA_R_64F,
+                                       w.p + kv.second[0]->w_off, CUDA_R_64F, dwork.p, dws,
+                                       hwork.data(), hws, einfo.p + io, nb));
+      io += nb;
+    }
+    cusolverDnDestroyParams(sp);
+  }
+  // ---- values to the host ---------------------------------------------------
+  std::vector<double> hs_small(n_small * kSmall), hs_j(js_total), hw(w_total);
+  std::vector<int> hinfo_s(n_small), hinfo_j(groups.size(), 0), hinfo_e(n_gram, 0);
+  if (n_small > 0) {
+    GQ_CUDA(cudaMemcpyAsync(hs_small.data(), ss.p, sizeof(double) * hs_small.size(),
                             cudaMemcpyDeviceToHost, s));
-    sync();
-    cusolverDnDestroyGesvdjInfo(prm);
-    for (int v : hinfo)
-      if (v != 0) fail(kSolverError, "gesvdj did not converge, info=" + std::to_string(v));
+    GQ_CUDA(cudaMemcpyAsync(hinfo_s.data(), sinfo.p, sizeof(int) * n_small,
+                            cudaMemcpyDeviceToHost, s));
+  }
+  if (js_total > 0) {
+    GQ_CUDA(cudaMemcpyAsync(hs_j.data(), js.p, sizeof(double) * js_total, cudaMemcpyDeviceToHost,
+                            s));
+    GQ_CUDA(cudaMemcpyAsync(hinfo_j.data(), jinfo.p, sizeof(int) * groups.size(),
+                            cudaMemcpyDeviceToHost, s));
+  }
+  if (w_total > 0) {
+    GQ_CUDA(cudaMemcpyAsync(hw.data(), w.p, sizeof(double) * w_total, cudaMemcpyDeviceToHost, s));
+    GQ_CUDA(cudaMemcpyAsync(hinfo_e.data(), einfo.p, sizeof(int) * n_gram,
+                            cudaMemcpyDeviceToHost, s));
+  }
+  sync();
+  cusolverDnDestroyGesvdjInfo(prm);
+  for (int v : hinfo_s)
+    if (v != 0) fail(kSolverError, "batched gesvdj did not converge, info=" + std::to_string(v));
+  for (int v : hinfo_j)
+    if (v != 0) fail(kSolverError, "gesvdj did not converge, info=" + std::to_string(v));
+  for (int v : hinfo_e)
+    if (v != 0) fail(kSolverError, "syevd failed, info=" + std::to_string(v));
+
+  // per-group descending values (p of them) and their source columns
+  for (Group *g : groups) {
+    g->svals.assign(g->p, 0.0);
+    g->src_cols.assign(g->p, 0);
+    if (g->route == kSmallJacobi) {
+      std::vector<int> idx(kSmall);
+      std::iota(idx.begin(), idx.end(), 0);
+      const double *sv0 = hs_small.data() + g->sv_off;
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return sv0[a] > sv0[b]; });
+      for (int64_t j = 0; j < g->p; ++j) {
+        g->src_cols[j] = idx[j];
+        g->svals[j] = sv0[idx[j]];
+      }
+    } else if (g->route == kJacobi) {
+      for (int64_t j = 0; j < g->p; ++j) {
+        g->src_cols[j] = (int)j;
+        g->svals[j] = hs_j[g->sv_off + j];
+      }
+    } else {
+      const double *lam = hw.data() + g->w_off;  // ascending
+      const double lmax = std::max(lam[g->dim - 1], 0.0);
+      for (int64_t j = 0; j < g->p; ++j) {
+        const int64_t c = g->dim - 1 - j;
+        g->src_cols[j] = (int)c;
+        const double l = lam[c];
+        g->svals[j] = (l > kGramZeroRtol * lmax) ? std::sqrt(l) : 0.0;
+      }
+    }
   }
 
-  // ---- global truncation on the host (s_total values) --------------------
-  std::vector<double> flat(s_total);
-  GQ_CUDA(cudaMemcpyAsync(flat.data(), sv.p, sizeof(double) * s_total, cudaMemcpyDeviceToHost, s));
-  sync();
+  // ---- global truncation on the host -----------------------------------------
+  std::vector<double> flat;
+  for (Group *g : groups) flat.insert(flat.end(), g->svals.begin(), g->svals.end());
   double smax = 0.0;
   for (double v : flat) smax = std::max(smax, v);
   for (double &v : flat)
     if (!(v > kZeroSvRtol * smax)) v = 0.0;
-  const int64_t ntot = s_total;
+  const int64_t ntot = (int64_t)flat.size();
   std::vector<int64_t> order(ntot);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
@@ -394,53 +613,118 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   SvdOut out;
   out.D = D;
   out.trunc_err = err;
-  std::vector<double> s_kept;        // per kept column, bond order
   std::vector<std::pair<QN, int64_t>> sectors;
-  int64_t lc_total = 0, rc_total = 0;
+  int64_t L_total = 0, R_total = 0, pos = 0;
   for (Group *g : groups) {
-    for (int64_t j = 0; j < g->p; ++j) {
-      const int64_t f = g->s_off + j;
-      if (flat[f] > 0.0) g->nnz++;
-      if (keep[f]) {
+    for (int64_t j = 0; j < g->p; ++j, ++pos) {
+      g->svals[j] = flat[pos];
+      if (flat[pos] > 0.0) g->nnz++;
+      if (keep[pos]) {
         g->keep++;
-        if (flat[f] > 0.0) g->keep_nz++;
+        if (flat[pos] > 0.0) g->keep_nz++;
       }
     }
     if (g->keep == 0) continue;
     g->sector = (int)sectors.size();
     sectors.push_back({g->q, g->keep});
-    const int64_t kz = g->keep - g->keep_nz;
-    g->lc_off = lc_total;
-    lc_total += g->m * kz;
-    g->rc_off = rc_total;
-    rc_total += g->n * kz;
+    g->L_off = L_total;
+    L_total += g->m * g->keep;
+    g->R_off = R_total;
+    R_total += g->n * g->keep;
   }
   GQ_CHECK(!sectors.empty(), "SVD kept no singular value");
 
-  // ---- sign convention on kept nonzero vectors ----------------------------
+  // ---- factors L (m x keep) and R (n x keep) per group ------------------------
+  // 'r' (scale_side 2): L = U, R = (S.Vt)^T; 'l' (1): L = U.S, R = V;
+  // plain (0): L = U, R = V.  Columns of kept zero values start at zero.
+  DevBuf Lb(L_total), Rb(R_total);
+  GQ_CUDA(cudaMemsetAsync(Lb.p, 0, sizeof(double) * L_total, s));
+  GQ_CUDA(cudaMemsetAsync(Rb.p, 0, sizeof(double) * R_total, s));
+  const bool scale_l = scale_side == 1, scale_r = scale_side == 2;
+  std::vector<ColItem> l_small, r_small, l_jac, r_jac, l_ev, r_ev;
+  for (Group *g : groups) {
+    for (int64_t j = 0; j < g->keep_nz; ++j) {
+      const int sc = g->src_cols[j];
+      const double sj = g->svals[j];
+      switch (g->route) {
+        case kSmallJacobi:
+        case kJacobi: {
+          auto &vl = g->route == kSmallJacobi ? l_small : l_jac;
+          auto &vr = g->route == kSmallJacobi ? r_small : r_jac;
+          vl.push_back({g->lv_off, g->L_off, (int)g->m, g->ld_l, (int)g->m, sc, (int)j,
+                        scale_l ? sj : 1.0});
+          vr.push_back({g->rv_off, g->R_off, (int)g->n, g->ld_r, (int)g->n, sc, (int)j,
+                        scale_r ? sj : 1.0});
+          break;
+        }
+        case kGramLeft:
+          l_ev.push_back({g->ev_off, g->L_off, (int)g->m, (int)g->dim, (int)g->m, sc, (int)j, 1.0});
+          break;
+        case kGramRight:
+          r_ev.push_back({g->ev_off, g->R_off, (int)g->n, (int)g->dim, (int)g->n, sc, (int)j, 1.0});
+          break;
+      }
+    }
+  }
+  launch_items(col_copy_kernel, l_small, sv.p, Lb.p);
+  launch_items(col_copy_kernel, r_small, su.p, Rb.p);
+  launch_items(col_copy_kernel, l_jac, jl.p, Lb.p);
+  launch_items(col_copy_kernel, r_jac, jr.p, Rb.p);
+  launch_items(col_copy_kernel, l_ev, ev.p, Lb.p);
+  launch_items(col_copy_kernel, r_ev, ev.p, Rb.p);
+  // projections for the Gram routes: R = X L (left) or L = X^T R (right)
+  {
+    const double one = 1.0, zero = 0.0;
+    for (Group *g : groups) {
+      if (g->keep_nz == 0) continue;
+      const int m = (int)g->m, n = (int)g->n, k = (int)g->keep_nz;
+      const double *X = mats.p + g->mat_off;
+      if (g->route == kGramLeft)
+        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, &one, X, n, Lb.p + g->L_off, m,
+                            &zero, Rb.p + g->R_off, n));
+      else if (g->route == kGramRight)
+        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, k, n, &one, X, n, Rb.p + g->R_off, n,
+                            &zero, Lb.p + g->L_off, m));
+    }
+  }
+  // sign convention on the kept nonzero columns (by the left factor)
   {
     std::vector<SignItem> items;
     for (Group *g : groups)
       for (int64_t j = 0; j < g->keep_nz; ++j)
-        items.push_back({g->lv_off + j * g->m, g->rv_off + j * g->n, (int)g->m, (int)g->n});
+        items.push_back({g->L_off + j * g->m, g->R_off + j * g->n, (int)g->m, (int)g->n});
     if (!items.empty()) {
       DevArray<SignItem> d;
       d.upload(items);
-      sign_fix_kernel<<<(unsigned)items.size(), 256, 0, s>>>(d.p, lv.p, rv.p);
+      sign_fix_kernel<<<(unsigned)items.size(), 256, 0, s>>>(d.p, Lb.p, Rb.p);
       GQ_CUDA(cudaGetLastError());
     }
   }
-  // ---- canonical completion for kept zeros ---------------------------------
-  DevBuf lcomp(lc_total), rcomp(rc_total);
-  for (Group *g : groups) {
+  // canonical completion of the kept zero values on the orthonormal side(s)
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    Group *g = groups[gi];
     const int64_t kz = g->keep - g->keep_nz;
     if (kz == 0) continue;
-    const int gidx = (int)(std::find(groups.begin(), groups.end(), g) - groups.begin());
-    null_completion(lv.p + g->lv_off, g->m, g->nnz, kz, gidx, 0, lcomp.p + g->lc_off);
-    null_completion(rv.p + g->rv_off, g->n, g->nnz, kz, gidx, 1, rcomp.p + g->rc_off);
+    auto completion = [&](bool left, double *dst) {
+      const int64_t dim = left ? g->m : g->n;
+      DevBuf q(std::max<int64_t>(dim * g->nnz, 1));
+      std::vector<ColItem> items;
+      const bool gram = g->route == kGramLeft || g->route == kGramRight;
+      for (int64_t j = 0; j < g->nnz; ++j)
+        items.push_back({gram ? g->ev_off : (left ? g->lv_off : g->rv_off), 0, (int)dim,
+                         gram ? (int)g->dim : (left ? g->ld_l : g->ld_r), (int)dim,
+                         g->src_cols[j], (int)j, 1.0});
+      const double *src = gram ? ev.p
+                               : g->route == kSmallJacobi ? (left ? sv.p : su.p)
+                                                          : (left ? jl.p : jr.p);
+      launch_items(col_copy_kernel, items, src, q.p);
+      null_completion(q.p, dim, g->nnz, kz, (int)gi, left ? 0 : 1, dst);
+    };
+    if (scale_side != 1) completion(true, Lb.p + g->L_off + g->keep_nz * g->m);
+    if (scale_side != 2) completion(false, Rb.p + g->R_off + g->keep_nz * g->n);
   }
 
-  // ---- output tensors --------------------------------------------------------
+  // ---- output tensors ---------------------------------------------------------
   Index nb;
   nb.dir = 1;
   for (auto &sq : sectors) {
@@ -456,6 +740,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   std::vector<std::vector<int>> ublocks, vblocks;
   for (Group *g : groups) {
     if (g->keep == 0) continue;
+    for (int64_t j = 0; j < g->keep; ++j) out.s.push_back(j < g->keep_nz ? g->svals[j] : 0.0);
     for (auto &rc : g->rows) {
       auto c = rc;
       c.push_back(g->sector);
@@ -471,67 +756,29 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   out.vt = make_structure(t.nq, vidx, t.div - ldiv, vblocks);
   out.u->allocate();
   out.vt->allocate();
-
-  // kept singular values per group (device) for the optional scaling
-  std::vector<double> kept_s;
-  std::vector<int64_t> ks_off(groups.size(), 0);
-  for (size_t gi = 0; gi < groups.size(); ++gi) {
-    Group *g = groups[gi];
-    ks_off[gi] = (int64_t)kept_s.size();
-    for (int64_t j = 0; j < g->keep; ++j) {
-      const double v = j < g->keep_nz ? flat[g->s_off + j] : 0.0;
-      kept_s.push_back(v);
-      out.s.push_back(v);
-    }
-  }
-  DevArray<double> ks;
-  ks.upload(kept_s.empty() ? std::vector<double>{0.0} : kept_s);
   {
     std::vector<ScatterItem> items;
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
-      Group *g = groups[gi];
+    for (Group *g : groups) {
       if (g->keep == 0) continue;
       for (size_t ri = 0; ri < g->rows.size(); ++ri) {
         auto c = g->rows[ri];
         c.push_back(g->sector);
         const int64_t ob = out.u->find(c.data());
-        ScatterItem it{};
-        it.dst_off = out.u->offs[ob];
-        it.rows = (int)g->rsz[ri];
-        it.k = (int)g->keep;
-        it.knz = (int)g->keep_nz;
-        it.mode = 0;
-        it.scale = scale_side == 1;
-        it.svd_off = g->lv_off + g->roff[ri];
-        it.ld_svd = (int)g->m;
-        it.comp_off = g->lc_off + g->roff[ri];
-        it.ld_comp = (int)g->m;
-        it.s_off = ks_off[gi];
-        items.push_back(it);
+        items.push_back({out.u->offs[ob], g->L_off + g->roff[ri], (int)g->rsz[ri], (int)g->keep,
+                         (int)g->m, 0});
       }
       for (size_t ci = 0; ci < g->cols.size(); ++ci) {
         std::vector<int> c{g->sector};
         c.insert(c.end(), g->cols[ci].begin(), g->cols[ci].end());
         const int64_t ob = out.vt->find(c.data());
-        ScatterItem it{};
-        it.dst_off = out.vt->offs[ob];
-        it.rows = (int)g->csz[ci];
-        it.k = (int)g->keep;
-        it.knz = (int)g->keep_nz;
-        it.mode = 1;
-        it.scale = scale_side == 2;
-        it.svd_off = g->rv_off + g->coff[ci];
-        it.ld_svd = (int)g->n;
-        it.comp_off = g->rc_off + g->coff[ci];
-        it.ld_comp = (int)g->n;
-        it.s_off = ks_off[gi];
-        items.push_back(it);
+        items.push_back({out.vt->offs[ob], g->R_off + g->coff[ci], (int)g->csz[ci], (int)g->keep,
+                         (int)g->n, 1});
       }
     }
     DevArray<ScatterItem> d;
     d.upload(items);
-    scatter_kernel<<<(unsigned)items.size(), 256, 0, s>>>(d.p, lv.p, rv.p, lcomp.p, rcomp.p, ks.p,
-                                                         out.u->data.p, out.vt->data.p);
+    scatter_kernel<<<(unsigned)items.size(), 256, 0, s>>>(d.p, Lb.p, Rb.p, out.u->data.p,
+                                                         out.vt->data.p);
     GQ_CUDA(cudaGetLastError());
   }
   return out;

@@ -104,26 +104,33 @@ def test_tc_matvec_matches_oracle(lib, where):
     assert rel_err(got, ref) <= TC_TOL
 
 
-def test_tc_dmrg_energy_close_to_fp64(lib):
-    """Heisenberg L=20, D=200 (the reference's CPU-runnable case), three
-    sweeps in each form from the same product state."""
+def test_tc_lanczos_energy_matches_fp64_same_problem(lib):
+    """Heisenberg L=20, D=200 (the reference's CPU-runnable case): take the
+    central effective Hamiltonian mid-sweep from an FP64 run and solve it in
+    both forms from the same start vector.  With the FP64 Rayleigh-quotient
+    correction the split form's energy agrees to 1e-9 relative."""
     from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS
-    from mps2_gb300.vmps import DMRGState, LanczosParams, SweepParams
+    from mps2_gb300.vmps import (Contract, DMRGState, LanczosParams, LanczosSolver,
+                                 SweepParams)
     N, D = 20, 200
     sv, mpo, qn0, _ = H.heisenberg_chain(N)
-    energies = {}
-    launches = {}
-    for prec in ("fp64", "tf32x3"):
-        mps = FiniteMPS(sv)
-        DirectStateInitMps(mps, H.neel_shuffled_labels(N, 0), qn0)
-        st = DMRGState(mps.tens, mpo)
-        st.init_envs(prec)
-        sp = SweepParams(3, D, D, 0.0, LanczosParams(1e-10, 100), precision=prec)
-        (e, _), n = tc_launches(lambda: st.sweep(sp))
-        energies[prec] = e
-        launches[prec] = n
-    assert launches["fp64"] == 0
-    assert launches["tf32x3"] > 0, "the tensor-core kernel did not run"
-    rel = abs(energies["tf32x3"] - energies["fp64"]) / abs(energies["fp64"])
-    print(f"E fp64 {energies['fp64']:.12f} tf32x3 {energies['tf32x3']:.12f} rel {rel:.2e}")
-    assert rel <= 1e-7
+    mps = FiniteMPS(sv)
+    DirectStateInitMps(mps, H.neel_shuffled_labels(N, 0), qn0)
+    st = DMRGState(mps.tens, mpo)
+    st.init_envs("fp64")
+    sp = SweepParams(3, D, D, 0.0, LanczosParams(1e-10, 100), precision="fp64")
+    st.sweep(sp)
+    c = N // 2 - 1
+    for i in range(c):
+        st.update(sp, "r", i)
+    L = st.get_env("l", c)
+    R = st.get_env("r", N - c - 2)
+    theta = Contract(st.get_mps(c), st.get_mps(c + 1), ([2], [0]))
+    eff = [L, mpo[c], mpo[c + 1], R]
+    lp = LanczosParams(1e-12, 100)
+    e64 = LanczosSolver(eff, theta, lp, "cent", precision="fp64").gs_eng
+    (res, n) = tc_launches(lambda: LanczosSolver(eff, theta, lp, "cent", precision="tf32x3"))
+    assert n > 0, "the tensor-core kernel did not run"
+    rel = abs(res.gs_eng - e64) / abs(e64)
+    print(f"E fp64 {e64:.14f} tf32x3 {res.gs_eng:.14f} rel {rel:.2e}")
+    assert rel <= 1e-9
