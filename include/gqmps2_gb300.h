@@ -212,6 +212,7 @@ int gq_dmrg_destroy(gq_dmrg *d);
 #define GQ_PROF_GEMM_TF32X3 1
 #define GQ_PROF_PERMUTE 2
 #define GQ_PROF_VECTOR 3
+#define GQ_PROF_SKINNY 4
 int gq_profile_enable(int on);
 int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes);
 /* The cudaStream_t all library work is queued on. */

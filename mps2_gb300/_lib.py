@@ -87,7 +87,7 @@ EXPORTS = {
     "gq_get_stream": (_I, [_PP]),
 }
 
-PROF = {"gemm_fp64": 0, "gemm_tf32x3": 1, "permute": 2, "vector": 3}
+PROF = {"gemm_fp64": 0, "gemm_tf32x3": 1, "permute": 2, "vector": 3, "skinny": 4}
 
 _lib: Optional[C.CDLL] = None
 

@@ -169,8 +169,10 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   const Tensor &o = *plan->out;
   const size_t nfa = free_a.size();
 
-  // Small B (an MPO tensor): the tall-skinny kernel reads A in place.
-  if (b.size() <= 65536) {
+  // Small B (an MPO tensor): the tall-skinny kernel reads A in place.  B
+  // must be small in absolute terms and tiny next to A, so a two-site state
+  // contracted with an environment never lands here.
+  if (skinny_eligible_sizes(a.size(), b.size())) {
     int64_t max_k = 0, max_n = 0;
     for (auto &kv : out) {
       int64_t n = 1;

@@ -30,7 +30,8 @@ enum ProfKernel : int {
   kProfGemmTf32 = 1,   // 3xTF32 tcgen05 grouped GEMM
   kProfPermute = 2,    // block permutes feeding the GEMMs
   kProfVector = 3,     // Lanczos vector kernels
-  kProfCount = 4,
+  kProfSkinny = 4,     // tall-skinny MPO-tensor contractions
+  kProfCount = 5,
 };
 bool prof_on();
 void prof_enable(bool on);
@@ -147,6 +148,7 @@ TensorPtr contract(const Tensor &a, const Tensor &b, const std::vector<int> &axe
 void cache_operand(ContractPlan &p, int which, const double *src);
 
 // Tall-skinny kernel (launched by run_contract when use_skinny).
+bool skinny_eligible_sizes(int64_t a_elems, int64_t b_elems);
 bool skinny_eligible(const Tensor &b, int64_t max_k, int64_t max_n);
 void launch_skinny(const ContractPlan &p, const double *A, const double *B, double *C);
 int skinny_rows_per_cta();

@@ -87,13 +87,17 @@ __global__ void __launch_bounds__(kSkRows)
 }
 }  // namespace
 
+bool skinny_eligible_sizes(int64_t a_elems, int64_t b_elems) {
+  return b_elems <= 16384 && 32 * b_elems <= a_elems;
+}
+
 bool skinny_eligible(const Tensor &b, int64_t max_k, int64_t max_n) {
-  return b.size() <= 65536 && max_k <= kSkMaxK && max_n <= 256;
+  return b.size() <= 16384 && max_k <= kSkMaxK && max_n <= 256;
 }
 
 void launch_skinny(const ContractPlan &p, const double *A, const double *B, double *C) {
   if (p.sk_nitems == 0) return;
-  prof_begin(kProfGemmFp64);
+  prof_begin(kProfSkinny);
   auto s = stream();
   const unsigned grid = (unsigned)p.sk_nitems;
   if (p.sk_jb == 8)
@@ -103,7 +107,7 @@ void launch_skinny(const ContractPlan &p, const double *A, const double *B, doub
   else
     skinny_kernel<32><<<grid, kSkRows, 0, s>>>(p.sk_items.p, p.sk_pairs.p, A, B, C);
   GQ_CUDA(cudaGetLastError());
-  prof_end(kProfGemmFp64, p.flops, 8.0 * (double)(p.a_elems + p.b_elems));
+  prof_end(kProfSkinny, p.flops, 8.0 * (double)(p.a_elems + p.b_elems));
 }
 
 int skinny_rows_per_cta() { return kSkRows; }
