@@ -44,7 +44,7 @@ SCHEDULE = [500, 800, 1100, 1400, 1700, 2000]
 L_SITES = 100
 LANCZOS = (1e-10, 100)
 WORKLOAD = "heisenberg_obc_L100_Sz0_D500to2000"
-FAMILIES = ("gemm_fp64", "gemm_tf32x3", "permute", "vector", "skinny")
+FAMILIES = ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc", "permute", "vector", "skinny")
 STRUCTURE_FIXTURE = os.path.join(ROOT, "tests", "golden", "bench_center_bond.json")
 
 
@@ -54,7 +54,9 @@ def _args():
     p.add_argument("--steps", type=int, default=1)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--precision", choices=["fp64", "tf32x3"], default="tf32x3")
+    p.add_argument("--precision", choices=["fp64", "tf32x3", "fp64tc"], default="tf32x3")
+    p.add_argument("--rayleigh", choices=["fp64", "fp64tc"], default="fp64tc",
+                   help="arithmetic of the split form's Rayleigh-quotient energies")
     p.add_argument("--schedule", default=",".join(map(str, SCHEDULE)),
                    help="comma-separated D per growth sweep; the last is the timed D")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -275,7 +277,7 @@ def run_ours(args):
     lp = LanczosParams(*LANCZOS)
 
     def params(d, prec=args.precision):
-        return SweepParams(1, d, d, 0.0, lp, precision=prec)
+        return SweepParams(1, d, d, 0.0, lp, precision=prec, rayleigh=args.rayleigh)
 
     mps, mpo = _model()
     st = DMRGState(mps.tens, mpo)
@@ -299,6 +301,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     profile_enable(True)
     clocks.start()
+    # an external profiler started with --profile-from-start off records the
+    # timed sweeps only
+    torch.cuda.profiler.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(ext)
@@ -309,6 +314,7 @@ def run_ours(args):
         energies.append(e0)
     ev1.record(ext)
     torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     prof = {k: profile_read(k) for k in FAMILIES}
@@ -347,17 +353,17 @@ def run_ours(args):
     theta = Contract(mpsd[c], mpsd[c + 1], ([2], [0]))
     eff = [envs[("l", c)], mpo[c], mpo[c + 1], envs[("r", L_SITES - c - 2)]]
     solve = {}
-    for prec in ("fp64", "tf32x3"):
+    for prec in ("fp64", "tf32x3", "fp64tc"):
         profile_enable(True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = LanczosSolver(eff, theta, lp, "cent", precision=prec)
+        r = LanczosSolver(eff, theta, lp, "cent", precision=prec, rayleigh=args.rayleigh)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         pr = {k: profile_read(k) for k in FAMILIES}
         profile_enable(False)
-        gemm_ms = sum(pr[k][1] for k in ("gemm_fp64", "gemm_tf32x3", "skinny"))
-        gemm_fl = sum(pr[k][2] for k in ("gemm_fp64", "gemm_tf32x3", "skinny"))
+        gemm_ms = sum(pr[k][1] for k in ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc", "skinny"))
+        gemm_fl = sum(pr[k][2] for k in ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc", "skinny"))
         solve[prec] = {"energy": r.gs_eng, "iters": r.iters, "seconds": dt,
                        "kernel_ms": {k: pr[k][1] for k in FAMILIES},
                        "matvec_gemm_tflops": gemm_fl / (gemm_ms * 1e-3) / 1e12 if gemm_ms else None,
@@ -392,6 +398,9 @@ def run_ours(args):
     fam = {"gemm_tf32x3": ("tensor", "TFLOP/s", 0.5 * peaks["bf16_tflops"],
                            f"half the {peak_kind} bf16 dense peak (the TF32 rate); useful flops"),
            "gemm_fp64": ("fp64", "TFLOP/s", fp64_peak, "cuBLAS DGEMM 8192^3 measured in this run"),
+           "gemm_fp64tc": ("tensor", "TFLOP/s", peaks["bf16_tflops"] / 28.0,
+                           f"the {peak_kind} bf16 dense peak / 28 (bf16 MMAs per FP64-accurate "
+                           "product); useful flops"),
            "permute": ("hbm", "GB/s", peaks["hbm_gbs"], f"{peak_kind} HBM copy bandwidth"),
            "vector": ("hbm", "GB/s", peaks["hbm_gbs"], f"{peak_kind} HBM copy bandwidth"),
            "skinny": ("hbm", "GB/s", peaks["hbm_gbs"], f"{peak_kind} HBM copy bandwidth")}

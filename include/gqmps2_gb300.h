@@ -49,6 +49,8 @@ extern "C" {
  * state).  Lanczos recurrence, tridiagonal solve and SVD are FP64 always. */
 #define GQ_PREC_FP64 0   /* plain form: FP64 end to end */
 #define GQ_PREC_TF32X3 1 /* split form: 3xTF32 tcgen05 products, FP64 sums */
+#define GQ_PREC_FP64TC 2 /* FP64-accurate tcgen05 products (exact bf16 digits,
+                            exact FP32 partial sums, FP64 merge) */
 
 /* Position of the two-site block (the reference's `where` string,
  * lanczos_solver_impl.h:93-112). */
@@ -63,6 +65,9 @@ typedef struct gq_dmrg gq_dmrg;
 typedef struct {
   double error;           /* default 1e-7 */
   int64_t max_iterations; /* default 200 */
+  int rayleigh; /* split form only (not in the reference): arithmetic of the
+                   Rayleigh-quotient energy of the ground state,
+                   GQ_PREC_FP64 (FP64 FMA) or GQ_PREC_FP64TC */
 } gq_lanczos_params;
 
 /* SweepParams (include/gqmps2/algorithm/vmps/two_site_update_finite_vmps.h:27-55)
@@ -204,6 +209,18 @@ int gq_dmrg_update(gq_dmrg *d, const gq_sweep_params *params, int dir, int targe
 int gq_dmrg_get_mps(gq_dmrg *d, int i, gq_tensor **out);
 int gq_dmrg_destroy(gq_dmrg *d);
 
+/* Batched instances ------------------------------------------------------ *
+ * Not in the reference (its tests run one chain per process).  Runs n
+ * independent DMRG states concurrently: a pool of `nthreads` host threads,
+ * each queueing its work on its own CUDA stream, takes the states in index
+ * order; for each state it builds the right environments if `init_envs`
+ * (in params[i].precision), then sweeps params[i].sweeps times.  e0[i]
+ * (optional) receives the energy of state i's last update.  The states must
+ * not be used by other calls meanwhile.  On failure the first error is
+ * returned; states not yet started are left untouched. */
+int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *params,
+                      int init_envs, int nthreads, double *e0);
+
 /* Measurement ------------------------------------------------------------ *
  * Not part of the reference (its only instrumentation is the Timer output,
  * lanczos_solver_impl.h:123-132).  CUDA-event timing of each kernel family
@@ -213,6 +230,7 @@ int gq_dmrg_destroy(gq_dmrg *d);
 #define GQ_PROF_PERMUTE 2
 #define GQ_PROF_VECTOR 3
 #define GQ_PROF_SKINNY 4
+#define GQ_PROF_GEMM_FP64TC 5
 int gq_profile_enable(int on);
 int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes);
 /* The cudaStream_t all library work is queued on. */

@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libgqmps2_gb300.so")
 GQ_OK = 0
 PREC_FP64 = 0
 PREC_TF32X3 = 1
+PREC_FP64TC = 2
 WHERE = {"lend": 0, "cent": 1, "rend": 2}
 
 
@@ -33,7 +34,7 @@ class GQError(RuntimeError):
 
 
 class LanczosParamsC(C.Structure):
-    _fields_ = [("error", C.c_double), ("max_iterations", C.c_int64)]
+    _fields_ = [("error", C.c_double), ("max_iterations", C.c_int64), ("rayleigh", C.c_int)]
 
 
 class SweepParamsC(C.Structure):
@@ -80,6 +81,7 @@ EXPORTS = {
     "gq_dmrg_get_env": (_I, [_P, _I, _I, _PP]),
     "gq_dmrg_sweep": (_I, [_P, C.POINTER(SweepParamsC), C.POINTER(UpdateStatsC), _DP]),
     "gq_dmrg_update": (_I, [_P, C.POINTER(SweepParamsC), _I, _I, C.POINTER(UpdateStatsC)]),
+    "gq_dmrg_run_batch": (_I, [C.POINTER(_P), _I, C.POINTER(SweepParamsC), _I, _I, _DP]),
     "gq_dmrg_get_mps": (_I, [_P, _I, _PP]),
     "gq_dmrg_destroy": (_I, [_P]),
     "gq_profile_enable": (_I, [_I]),
@@ -87,7 +89,8 @@ EXPORTS = {
     "gq_get_stream": (_I, [_PP]),
 }
 
-PROF = {"gemm_fp64": 0, "gemm_tf32x3": 1, "permute": 2, "vector": 3, "skinny": 4}
+PROF = {"gemm_fp64": 0, "gemm_tf32x3": 1, "permute": 2, "vector": 3, "skinny": 4,
+        "gemm_fp64tc": 5}
 
 _lib: Optional[C.CDLL] = None
 

@@ -1,8 +1,11 @@
 // C ABI (include/gqmps2_gb300.h) over the library's C++ internals.
 #include "../../include/gqmps2_gb300.h"
 
+#include <atomic>
 #include <cstdio>
+#include <mutex>
 #include <string>
+#include <thread>
 
 #include "gq_dmrg.hpp"
 
@@ -35,7 +38,13 @@ int guarded(F &&f) {
 }
 
 gq::Precision prec_of(int p) {
-  GQ_CHECK(p == GQ_PREC_FP64 || p == GQ_PREC_TF32X3, "unknown precision");
+  GQ_CHECK(p == GQ_PREC_FP64 || p == GQ_PREC_TF32X3 || p == GQ_PREC_FP64TC, "unknown precision");
+  return (gq::Precision)p;
+}
+
+gq::Precision rayleigh_of(int p) {
+  GQ_CHECK(p == GQ_PREC_FP64 || p == GQ_PREC_FP64TC,
+           "the Rayleigh-quotient energy needs an FP64-accurate form");
   return (gq::Precision)p;
 }
 
@@ -227,6 +236,7 @@ int gq_lanczos(const gq_tensor *L, const gq_tensor *Wl, const gq_tensor *Wr, con
     gq::LanczosParamsC lp;
     lp.error = params->error;
     lp.max_iterations = params->max_iterations;
+    lp.rayleigh = rayleigh_of(params->rayleigh);
     auto res = gq::lanczos(h, *space, lp, prec_of(precision));
     gq::check_device_errors();
     if (iters) *iters = res.iters;
@@ -313,6 +323,7 @@ gq::SweepParamsC sweep_params(const gq_sweep_params *p) {
   sp.lanczos.max_iterations = p->lanczos.max_iterations;
   sp.precision = prec_of(p->precision);
   sp.verbose = p->verbose;
+  sp.lanczos.rayleigh = rayleigh_of(p->lanczos.rayleigh);
   return sp;
 }
 
@@ -349,6 +360,58 @@ int gq_dmrg_sweep(gq_dmrg *d, const gq_sweep_params *p, gq_update_stats *stats, 
     if (stats)
       for (size_t i = 0; i < st.size(); ++i) export_stats(st[i], stats[i]);
     if (e0) *e0 = e;
+  });
+}
+
+int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *params,
+                      int init_envs, int nthreads, double *e0) {
+  return guarded([&] {
+    GQ_CHECK(n >= 0 && (n == 0 || (states && params)), "bad arguments");
+    GQ_CHECK(nthreads >= 1, "nthreads must be positive");
+    for (int i = 0; i < n; ++i) {
+      GQ_CHECK(states[i], "null dmrg handle");
+      sweep_params(&params[i]);  // validate up front
+    }
+    gq::sync();  // the states were built on this thread's lane
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    std::mutex mu;
+    int err_code = GQ_OK;
+    std::string err_msg;
+    auto worker = [&] {
+      gq::Lane *l = nullptr;
+      const int rc = guarded([&] {
+        l = gq::lane_create();
+        gq::lane_bind(l);
+        for (int i = next++; i < n && !failed; i = next++) {
+          const gq::SweepParamsC sp = sweep_params(&params[i]);
+          gq::Dmrg &d = states[i]->d;
+          if (init_envs) d.init_envs(sp.precision);
+          double e = 0.0;
+          for (int64_t s = 0; s < sp.sweeps; ++s) e = d.sweep(sp, nullptr);
+          gq::check_device_errors();
+          if (e0) e0[i] = e;
+        }
+      });
+      if (rc != GQ_OK) {
+        failed = true;
+        std::lock_guard<std::mutex> lk(mu);
+        if (err_code == GQ_OK) {
+          err_code = rc;
+          err_msg = gq_last_error();
+        }
+      }
+      if (l) {
+        gq::lane_bind(nullptr);
+        gq::lane_destroy(l);
+      }
+    };
+    const int nt = std::max(1, std::min(nthreads, n));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    if (n > 0) worker();
+    for (auto &th : pool) th.join();
+    if (err_code != GQ_OK) throw gq::Error(err_code, "batched run: " + err_msg);
   });
 }
 

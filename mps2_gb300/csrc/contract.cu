@@ -276,16 +276,20 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
     for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
     for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
     bool tc = false;
-    if (prec == kTF32x3) {
+    if (prec == kTF32x3 || prec == kFP64TC) {
+      // FP64-accurate form: 128 x 96 tiles, about 35 times the FP64 rate
+      const int TM = prec == kTF32x3 ? 128 : oz_tile_m();
+      const int TN = prec == kTF32x3 ? 128 : oz_tile_n();
+      const double frac = prec == kTF32x3 ? 0.02 : 0.03;
       double useful = 0.0, padded = 0.0;
       for (auto &cp : kv.second) {
         int64_t k = 1;
         for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
         useful += 2.0 * m * n * k;
-        padded += 2.0 * ((m + 127) / 128 * 128.0) * ((n + 127) / 128 * 128.0) *
+        padded += 2.0 * (double)((m + TM - 1) / TM * TM) * (double)((n + TN - 1) / TN * TN) *
                   ((k + 31) / 32 * 32.0);
       }
-      tc = useful >= 0.02 * padded;
+      tc = useful >= frac * padded;
       if (tc) plan->padded_flops += padded;
     }
     any_tc |= tc;
@@ -296,10 +300,16 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   for (int64_t ob = 0; ob < o.nblocks(); ++ob)
     if (!touched[ob]) { any_fp = true; plan->nzero_blocks++; }
 
-  plan->use_tc = any_tc;
-  if (any_tc) {
+  const bool oz = prec == kFP64TC;
+  plan->use_tc = any_tc && !oz;
+  plan->use_oz = any_tc && oz;
+  if (plan->use_tc) {
     build_tc_pack(a, free_a, axes_a, plan->ta);
     build_tc_pack(b, free_b, axes_b, plan->tb);
+  }
+  if (plan->use_oz) {
+    build_oz_pack(a, free_a, axes_a, oz_tile_m(), plan->oa);
+    build_oz_pack(b, free_b, axes_b, oz_tile_n(), plan->ob);
   }
   if (any_fp) {
     if (is_identity(pa)) {
@@ -322,6 +332,8 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
 
   std::vector<GemmTile> tiles, tiles_tc;
   std::vector<GemmPair> pairs, pairs_tc;
+  std::vector<OzTile> tiles_oz;
+  std::vector<OzPair> pairs_oz;
   auto add_tiles = [](std::vector<GemmTile> &dst, int64_t c_off, int64_t m, int64_t n, int pbeg,
                       int pend, int64_t ksum, int TM, int TN) {
     for (int64_t r0 = 0; r0 < m; r0 += TM)
@@ -339,6 +351,38 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
       }
   };
   for (auto &b0 : obs) {
+    if (b0.tc && oz) {
+      const int pbeg = (int)pairs_oz.size();
+      int64_t ksum = 0;
+      for (auto &cp : *b0.pairs) {
+        int64_t k = 1;
+        for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
+        pairs_oz.push_back({plan->oa.base[cp.ablk], plan->ob.base[cp.bblk], (int)k, 0});
+        ksum += k;
+        const double f = 2.0 * (double)b0.m * (double)b0.n * (double)k;
+        plan->flops += f;
+        plan->flops_oz += f;
+      }
+      const auto &cp0 = (*b0.pairs)[0];
+      const int ar = plan->oa.row_base[cp0.ablk], br = plan->ob.row_base[cp0.bblk];
+      const int TM = oz_tile_m(), TN = oz_tile_n();
+      for (int64_t r0 = 0; r0 < b0.m; r0 += TM)
+        for (int64_t c0 = 0; c0 < b0.n; c0 += TN) {
+          OzTile t{};
+          t.c_off = o.offs[b0.ob];
+          t.m = (int)b0.m;
+          t.n = (int)b0.n;
+          t.row0 = (int)r0;
+          t.col0 = (int)c0;
+          t.pair_begin = pbeg;
+          t.pair_end = (int)pairs_oz.size();
+          t.a_rbase = ar;
+          t.b_rbase = br;
+          t.work = ksum * std::min<int64_t>(TM, b0.m - r0) * std::min<int64_t>(TN, b0.n - c0);
+          tiles_oz.push_back(t);
+        }
+      continue;
+    }
     auto &pl = b0.tc ? pairs_tc : pairs;
     const int pbeg = (int)pl.size();
     int64_t ksum = 0;
@@ -376,6 +420,11 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   auto by_work = [](const GemmTile &x, const GemmTile &y) { return x.work > y.work; };
   std::stable_sort(tiles.begin(), tiles.end(), by_work);
   std::stable_sort(tiles_tc.begin(), tiles_tc.end(), by_work);
+  std::stable_sort(tiles_oz.begin(), tiles_oz.end(),
+                   [](const OzTile &x, const OzTile &y) { return x.work > y.work; });
+  plan->ntiles_oz = (int64_t)tiles_oz.size();
+  plan->tiles_oz.upload(tiles_oz);
+  plan->pairs_oz.upload(pairs_oz);
   plan->tile_m = gemm_tile_m(any_tc ? kTF32x3 : kFP64);
   plan->tile_n = gemm_tile_n(any_tc ? kTF32x3 : kFP64);
   plan->ntiles = (int64_t)tiles.size();
@@ -402,11 +451,26 @@ int64_t contract_scratch(const ContractPlan &p) {
   if (p.use_tc)
     s += (p.a_cached ? 0 : floats_as_doubles(p.ta.floats)) +
          (p.b_cached ? 0 : floats_as_doubles(p.tb.floats));
+  if (p.use_oz)
+    s += (p.a_oz_cached ? 0 : oz_pack_doubles(p.oa)) + (p.b_oz_cached ? 0 : oz_pack_doubles(p.ob));
   return s;
 }
 
 void cache_operand(ContractPlan &p, int which, const double *src) {
-  if (!p.use_tc || p.use_skinny) return;
+  if (p.use_skinny) return;
+  if (p.use_oz) {
+    if (which == 0) {
+      p.a_oz.alloc(oz_pack_doubles(p.oa));
+      run_oz_pack(p.oa, src, oz_layout(p.oa, p.a_oz.p));
+      p.a_oz_cached = true;
+    } else {
+      p.b_oz.alloc(oz_pack_doubles(p.ob));
+      run_oz_pack(p.ob, src, oz_layout(p.ob, p.b_oz.p));
+      p.b_oz_cached = true;
+    }
+    return;
+  }
+  if (!p.use_tc) return;
   if (which == 0) {
     p.a_packed.alloc(floats_as_doubles(p.ta.floats));
     run_tc_pack(p.ta, src, align16(p.a_packed.p));
@@ -442,6 +506,24 @@ void run_contract(const ContractPlan &p, const double *a, const double *b, doubl
       s += floats_as_doubles(p.tb.floats);
     }
     launch_gemm_tf32x3(p, A, B, c);
+  }
+  if (p.use_oz && p.ntiles_oz > 0) {
+    OzPacked A, B;
+    if (p.a_oz_cached) {
+      A = oz_layout(p.oa, const_cast<double *>(p.a_oz.p));
+    } else {
+      A = oz_layout(p.oa, s);
+      run_oz_pack(p.oa, a, A);
+      s += oz_pack_doubles(p.oa);
+    }
+    if (p.b_oz_cached) {
+      B = oz_layout(p.ob, const_cast<double *>(p.b_oz.p));
+    } else {
+      B = oz_layout(p.ob, s);
+      run_oz_pack(p.ob, b, B);
+      s += oz_pack_doubles(p.ob);
+    }
+    launch_gemm_fp64tc(p, A, B, c);
   }
   if (p.ntiles == 0) return;
   const double *A = a, *B = b;

@@ -15,7 +15,15 @@
 
 namespace gq {
 
-void Dmrg::init_envs(Precision prec) {
+// Arithmetic of the environment contractions.  An environment's error goes
+// into every later energy at first order (E = <psi|L W W R|psi>), so the
+// split form grows its environments FP64-accurately, on the tensor cores;
+// only the matvec, whose error reaches the energy at second order through
+// the Rayleigh quotient, runs in 3xTF32.
+Precision env_precision(Precision prec) { return prec == kTF32x3 ? kFP64TC : prec; }
+
+void Dmrg::init_envs(Precision prec_in) {
+  const Precision prec = env_precision(prec_in);
   const int Nn = N();
   GQ_CHECK(Nn >= 2, "DMRG needs at least two sites");
   TensorPtr renv;
@@ -82,6 +90,7 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
   const auto t0 = clk::now();
   const int Nn = N();
   const Precision prec = prm.precision;
+  const Precision envp = env_precision(prec);
   const Classified c = classify(Nn, dir, target);
   UpdateStatsC st{};
   st.site = target;
@@ -113,6 +122,7 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
   LanczosParamsC lp;
   lp.error = prm.lanczos.error;
   lp.max_iterations = prm.lanczos.max_iterations;
+  lp.rayleigh = prm.lanczos.rayleigh;
   auto res = lanczos(h, *space, lp, prec);
   sync();
   st.lanczos_seconds = seconds_since(tl);
@@ -141,12 +151,12 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
       const Tensor &A = *mps[target];
       auto Ad = dag(A);
       if (target == 0) {
-        auto temp = contract(A, *mpo[target], {0}, {0}, prec, &f1);
-        envs[{'l', c.lenv_len + 1}] = contract(*temp, *Ad, {2}, {0}, prec, &f2);
+        auto temp = contract(A, *mpo[target], {0}, {0}, envp, &f1);
+        envs[{'l', c.lenv_len + 1}] = contract(*temp, *Ad, {2}, {0}, envp, &f2);
       } else {
-        auto t1 = contract(*h.L, A, {0}, {0}, prec, &f1);
-        auto t2 = contract(*t1, *mpo[target], {0, 2}, {0, 1}, prec, &f2);
-        envs[{'l', c.lenv_len + 1}] = contract(*t2, *Ad, {0, 2}, {0, 1}, prec, &f3);
+        auto t1 = contract(*h.L, A, {0}, {0}, envp, &f1);
+        auto t2 = contract(*t1, *mpo[target], {0, 2}, {0, 1}, envp, &f2);
+        envs[{'l', c.lenv_len + 1}] = contract(*t2, *Ad, {0, 2}, {0, 1}, envp, &f3);
       }
     }
   } else {
@@ -154,12 +164,12 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
       const Tensor &A = *mps[target];
       auto Ad = dag(A);
       if (target == Nn - 1) {
-        auto temp = contract(A, *mpo[target], {1}, {0}, prec, &f1);
-        envs[{'r', c.renv_len + 1}] = contract(*temp, *Ad, {2}, {1}, prec, &f2);
+        auto temp = contract(A, *mpo[target], {1}, {0}, envp, &f1);
+        envs[{'r', c.renv_len + 1}] = contract(*temp, *Ad, {2}, {1}, envp, &f2);
       } else {
-        auto t1 = contract(A, *h.R, {2}, {0}, prec, &f1);
-        auto t2 = contract(*t1, *mpo[target], {1, 2}, {1, 3}, prec, &f2);
-        envs[{'r', c.renv_len + 1}] = contract(*t2, *Ad, {3, 1}, {1, 2}, prec, &f3);
+        auto t1 = contract(A, *h.R, {2}, {0}, envp, &f1);
+        auto t2 = contract(*t1, *mpo[target], {1, 2}, {1, 3}, envp, &f2);
+        envs[{'r', c.renv_len + 1}] = contract(*t2, *Ad, {3, 1}, {1, 2}, envp, &f3);
       }
     }
   }

@@ -519,7 +519,7 @@ void launch_gemm_tf32x3(const ContractPlan &p, const float *A, const float *B, d
                                  (int)smem));
     attr = true;
   }
-  int *err = reinterpret_cast<int *>(ctx().dev_scalars + 63);
+  int *err = tc_error_flag();
   prof_begin(kProfGemmTf32);
   gemm_tf32x3_kernel<<<(unsigned)p.ntiles_tc, tc::kThreads, smem, stream()>>>(
       p.tiles_tc.p, p.pairs_tc.p, A, B, C, err);
@@ -527,6 +527,6 @@ void launch_gemm_tf32x3(const ContractPlan &p, const float *A, const float *B, d
   prof_end(kProfGemmTf32, p.flops_tc, 8.0 * (double)(p.a_elems + p.b_elems));
 }
 
-int *tc_error_flag() { return reinterpret_cast<int *>(ctx().dev_scalars + 63); }
+int *tc_error_flag() { return reinterpret_cast<int *>(lane().dev_scalars + 63); }
 
 }  // namespace gq

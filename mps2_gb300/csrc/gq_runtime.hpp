@@ -10,18 +10,34 @@
 
 namespace gq {
 
+// An execution lane: the stream a host thread's library work is queued on,
+// with the scalar buffers and library handles tied to that stream.  Every
+// thread uses the context's main lane unless it has bound its own, which
+// is how independent DMRG instances run concurrently (one host thread and
+// one stream each).
+struct Lane {
+  cudaStream_t stream = nullptr;
+  double *host_scalars = nullptr;  // pinned, 64 doubles
+  double *dev_scalars = nullptr;   // device, 64 doubles; [63] = tensor-core error word
+  void *cusolver = nullptr;        // cusolverDnHandle_t, created lazily
+  void *cublas = nullptr;          // cublasHandle_t, created lazily
+};
+
 struct Context {
   int device = 0;
   cudaDeviceProp prop{};
-  cudaStream_t stream = nullptr;
-  double *host_scalars = nullptr;  // pinned, 64 doubles
-  double *dev_scalars = nullptr;   // device, 64 doubles
-  cudaEvent_t sync_event = nullptr;
-  void *cusolver = nullptr;        // cusolverDnHandle_t, created lazily
+  Lane main;
 };
 
 Context &ctx();
 void init_context(int device);
+void init_lane(Lane &l);
+void destroy_lane_handles(Lane &l);  // cuSOLVER / cuBLAS handles (svd.cu)
+Lane &lane();              // this thread's lane
+Lane *lane_create();       // a new lane (own non-blocking stream)
+void lane_destroy(Lane *l);
+void lane_bind(Lane *l);   // bind to this thread (nullptr: the main lane)
+bool on_main_lane();
 void sync();
 
 // Kernel profiling with CUDA events on the library stream (off by default).
@@ -31,7 +47,8 @@ enum ProfKernel : int {
   kProfPermute = 2,    // block permutes feeding the GEMMs
   kProfVector = 3,     // Lanczos vector kernels
   kProfSkinny = 4,     // tall-skinny MPO-tensor contractions
-  kProfCount = 5,
+  kProfGemmFp64Tc = 5, // FP64-accurate exact-slice tcgen05 grouped GEMM
+  kProfCount = 6,
 };
 bool prof_on();
 void prof_enable(bool on);
@@ -44,6 +61,8 @@ enum Precision : int {
   kFP64 = 0,    // FP64 FMA end to end
   kTF32x3 = 1,  // 3xTF32 split products on tcgen05, FP32 accumulate per
                 // K-chunk, FP64 sum of the chunks
+  kFP64TC = 2,  // FP64-accurate products on tcgen05: exact bf16 integer
+                // digits of the operands, exact FP32 partial sums
 };
 
 // ---------------------------------------------------------------------------
@@ -101,6 +120,26 @@ struct TcPackPlan {
   DevArray<char> blocks_dev, tasks_dev;
 };
 
+// FP64-accurate tensor-core form (gemm_fp64tc.cu): operands packed as 7
+// bf16 digit images per 32-k tile plus one scale exponent per operand row.
+struct OzTile {
+  int64_t c_off;
+  int m, n, row0, col0;
+  int pair_begin, pair_end;
+  int a_rbase, b_rbase;  // first operand row of the output block in A / B
+  int64_t work;
+};
+struct OzPair { int64_t a_off, b_off; int k, pad; };
+struct OzPackPlan {
+  std::vector<int64_t> base;  // byte offset of each block's tile images
+  std::vector<int> row_base;  // operand row of each block's row 0
+  int64_t bytes = 0;
+  int nrows = 0;
+  int64_t ntasks = 0;
+  DevArray<char> blocks_dev, tasks_dev;
+};
+struct OzPacked { unsigned char *data = nullptr; int *rowexp = nullptr; };
+
 struct ContractPlan {
   TensorPtr out;          // output structure (no data)
   int transA = 0, transB = 0;
@@ -122,6 +161,14 @@ struct ContractPlan {
   DevArray<GemmPair> pairs_tc;    // offsets into the packed operands
   int64_t ntiles_tc = 0;
   double flops_tc = 0.0;
+  bool use_oz = false;    // FP64-accurate tcgen05 kernel for some blocks
+  OzPackPlan oa, ob;
+  bool a_oz_cached = false, b_oz_cached = false;
+  DevBuf a_oz, b_oz;
+  DevArray<OzTile> tiles_oz;
+  DevArray<OzPair> pairs_oz;
+  int64_t ntiles_oz = 0;
+  double flops_oz = 0.0;
   int64_t nzero_blocks = 0;   // output blocks with no contribution
   DevArray<int64_t> zero_blocks;  // (offset, size) pairs to clear
   double flops = 0.0;         // 2*m*n*k summed over block products
@@ -156,6 +203,14 @@ int skinny_rows_per_cta();
 // GEMM kernels (launched by run_contract)
 void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, double *C);
 void launch_gemm_tf32x3(const ContractPlan &p, const float *A, const float *B, double *C);
+void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
+                   const std::vector<int> &k_legs, int tile_rows, OzPackPlan &pp);
+int64_t oz_pack_doubles(const OzPackPlan &pp);
+OzPacked oz_layout(const OzPackPlan &pp, double *buf);
+void run_oz_pack(const OzPackPlan &pp, const double *src, const OzPacked &dst);
+void launch_gemm_fp64tc(const ContractPlan &p, const OzPacked &A, const OzPacked &B, double *C);
+int oz_tile_m();
+int oz_tile_n();
 void build_tc_pack(const Tensor &t, const std::vector<int> &row_legs,
                    const std::vector<int> &k_legs, TcPackPlan &pp);
 void run_tc_pack(const TcPackPlan &pp, const double *src, float *dst);
@@ -235,8 +290,10 @@ struct LanczosParamsC {
   double error = 1e-7;
   int64_t max_iterations = 200;
   // Split form only: recompute the reported energy as the FP64 Rayleigh
-  // quotient <gs|H|gs>/<gs|gs> with one FP64 matvec.
+  // quotient <gs|H|gs>/<gs|gs> with one matvec in an FP64-accurate form
+  // (kFP64 or kFP64TC).
   bool fp64_rayleigh = true;
+  Precision rayleigh = kFP64;
 };
 struct LanczosResult {
   int64_t iters = 0;

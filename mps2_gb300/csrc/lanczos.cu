@@ -159,7 +159,7 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   double *a_dev = sc.p, *n_dev = sc.p + maxit;
   DevBuf red(dot_scratch_elems());
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
-  double *hs = ctx().host_scalars;
+  double *hs = lane().host_scalars;
 
   auto matvec = [&](const double *x) {
     run_matvec(*plan, x, last.p);
@@ -216,7 +216,7 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
     res.gs = gs;
     if (prec == kTF32x3 && prm.fp64_rayleigh) {
       // FP64 Rayleigh quotient of the split-precision ground state
-      auto p64 = plan_matvec(h, init, kFP64);
+      auto p64 = plan_matvec(h, init, prm.rayleigh);
       run_matvec(*p64, gs->data.p, last.p);
       dev_dot(gs->data.p, last.p, n, a_dev, red.p);
       dev_dot(gs->data.p, gs->data.p, n, n_dev, red.p);

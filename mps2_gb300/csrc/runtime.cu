@@ -35,21 +35,54 @@ void init_context(int device) {
   if (c->prop.major < 10)
     fail(kCudaError, "this library is built for sm_103a (GB300); found sm_" +
                          std::to_string(c->prop.major) + std::to_string(c->prop.minor));
-  GQ_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   // Keep freed blocks cached in the pool: tensors are created and released
   // at every two-site update.
   cudaMemPool_t pool;
   GQ_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
   uint64_t thr = UINT64_MAX;
   GQ_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-  GQ_CUDA(cudaMallocHost((void **)&c->host_scalars, sizeof(double) * 64));
-  GQ_CUDA(cudaMallocAsync((void **)&c->dev_scalars, sizeof(double) * 64, c->stream));
-  GQ_CUDA(cudaMemsetAsync(c->dev_scalars, 0, sizeof(double) * 64, c->stream));
-  GQ_CUDA(cudaEventCreateWithFlags(&c->sync_event, cudaEventDisableTiming));
+  init_lane(c->main);
   g_ctx = c;
 }
 
-cudaStream_t stream() { return ctx().stream; }
+namespace {
+thread_local Lane *t_lane = nullptr;
+}  // namespace
+
+void init_lane(Lane &l) {
+  GQ_CUDA(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking));
+  GQ_CUDA(cudaMallocHost((void **)&l.host_scalars, sizeof(double) * 64));
+  GQ_CUDA(cudaMallocAsync((void **)&l.dev_scalars, sizeof(double) * 64, l.stream));
+  GQ_CUDA(cudaMemsetAsync(l.dev_scalars, 0, sizeof(double) * 64, l.stream));
+  GQ_CUDA(cudaStreamSynchronize(l.stream));
+}
+
+Lane &lane() { return t_lane ? *t_lane : ctx().main; }
+
+Lane *lane_create() {
+  ctx();
+  auto *l = new Lane();
+  init_lane(*l);
+  return l;
+}
+
+void lane_destroy(Lane *l) {
+  if (!l) return;
+  if (t_lane == l) t_lane = nullptr;
+  cudaStreamSynchronize(l->stream);
+  if (l->cusolver || l->cublas) destroy_lane_handles(*l);
+  cudaFreeAsync(l->dev_scalars, l->stream);
+  cudaStreamSynchronize(l->stream);
+  cudaFreeHost(l->host_scalars);
+  cudaStreamDestroy(l->stream);
+  delete l;
+}
+
+void lane_bind(Lane *l) { t_lane = l; }
+
+bool on_main_lane() { return t_lane == nullptr; }
+
+cudaStream_t stream() { return lane().stream; }
 
 void sync() { GQ_CUDA(cudaStreamSynchronize(stream())); }
 
@@ -108,7 +141,9 @@ void prof_drain() {
 }
 }  // namespace
 
-bool prof_on() { return g_prof.on; }
+// The profiler's counters are process-wide and filled from the main lane
+// only; work on other lanes is not profiled.
+bool prof_on() { return g_prof.on && on_main_lane(); }
 
 void prof_enable(bool on) {
   prof_drain();
@@ -120,14 +155,14 @@ void prof_enable(bool on) {
 }
 
 void prof_begin(ProfKernel k) {
-  if (!g_prof.on) return;
+  if (!prof_on()) return;
   auto e = prof_event();
   GQ_CUDA(cudaEventRecord(e, stream()));
   g_prof.open[k] = e;
 }
 
 void prof_end(ProfKernel k, double flops, double bytes) {
-  if (!g_prof.on || !g_prof.open[k]) return;
+  if (!prof_on() || !g_prof.open[k]) return;
   auto e = prof_event();
   GQ_CUDA(cudaEventRecord(e, stream()));
   g_prof.pending.push_back({(int)k, g_prof.open[k], e, flops, bytes});

@@ -26,8 +26,14 @@
 //    eigenvectors of the Gram matrix on that side (syevd) and the other
 //    factor comes by projection without dividing by singular values --
 //    'r' updates: U from Theta Theta^T and S.Vt = U^T Theta; 'l' updates:
-//    V from Theta^T Theta and U.S = Theta V.  The Gram matrices are solved
-//    in size buckets with one batched eigensolve per bucket.  On these
+//    V from Theta^T Theta and U.S = Theta V.  When the other side is much
+//    smaller (at most 0.7x, canonical side >= 256), the eigensolve runs on
+//    the other side's Gram matrix instead and the canonical factor is the
+//    projection through it, column-normalised and orthonormalised by
+//    CholeskyQR2 ('r': U = qr(Theta V), 'l': V = qr(Theta^T U)); the
+//    eigensolve, not the projections, dominates at these sizes.  The Gram
+//    matrices are solved in size buckets with one batched eigensolve per
+//    bucket.  On these
 //    groups eigenvalues below 1e-14 of the group's largest are the
 //    eigensolver's noise floor and count as exact zeros (singular values
 //    below ~1e-7 of the group's largest);
@@ -65,23 +71,27 @@ enum Route { kSmallJacobi = 0, kJacobi = 1, kGramLeft = 2, kGramRight = 3 };
                                          std::to_string((int)s_));                    \
   } while (0)
 
+// Library handles of this thread's lane, bound to the lane's stream.
 cusolverDnHandle_t solver() {
-  auto &c = ctx();
-  if (!c.cusolver) {
+  auto &l = lane();
+  if (!l.cusolver) {
     cusolverDnHandle_t h;
     GQ_SOLVER(cusolverDnCreate(&h));
-    c.cusolver = h;
+    GQ_SOLVER(cusolverDnSetStream(h, l.stream));
+    l.cusolver = h;
   }
-  auto h = (cusolverDnHandle_t)c.cusolver;
-  GQ_SOLVER(cusolverDnSetStream(h, c.stream));
-  return h;
+  return (cusolverDnHandle_t)l.cusolver;
 }
 
 cublasHandle_t blas() {
-  static cublasHandle_t h = nullptr;
-  if (!h) GQ_BLAS(cublasCreate(&h));
-  GQ_BLAS(cublasSetStream(h, stream()));
-  return h;
+  auto &l = lane();
+  if (!l.cublas) {
+    cublasHandle_t h;
+    GQ_BLAS(cublasCreate(&h));
+    GQ_BLAS(cublasSetStream(h, l.stream));
+    l.cublas = h;
+  }
+  return (cublasHandle_t)l.cublas;
 }
 
 // ---------------------------------------------------------------------------
@@ -223,6 +233,69 @@ void launch_items(void (*kern)(const T *, const double *, double *), const std::
   GQ_CUDA(cudaGetLastError());
 }
 
+// Column normalisation: each of the k columns (dim entries, ld dim) scaled
+// to unit 2-norm (zero columns stay zero).  One CTA per column.
+__global__ void normalise_columns_kernel(double *__restrict__ q, int dim) {
+  double *c = q + (int64_t)blockIdx.x * dim;
+  __shared__ double part[256];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < dim; i += blockDim.x) acc = fma(c[i], c[i], acc);
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
+    __syncthreads();
+  }
+  const double nrm2 = part[0];
+  if (nrm2 <= 0.0) return;
+  const double inv = 1.0 / sqrt(nrm2);
+  for (int i = threadIdx.x; i < dim; i += blockDim.x) c[i] *= inv;
+}
+
+void normalise_columns(double *q, int64_t dim, int64_t k) {
+  if (k == 0) return;
+  normalise_columns_kernel<<<(unsigned)k, 256, 0, stream()>>>(q, (int)dim);
+  GQ_CUDA(cudaGetLastError());
+}
+
+// CholeskyQR2: the k columns of q (dim x k, ld dim) replaced by an
+// orthonormal basis of their span (q <- q R^-1 twice, R from the Cholesky
+// factor of q^T q).
+void cholqr2(double *q, int64_t dim, int64_t k) {
+  if (k == 0) return;
+  auto s = stream();
+  auto bh = blas();
+  auto sh = solver();
+  const int d = (int)dim, kk = (int)k;
+  const double one = 1.0, zero = 0.0;
+  DevBuf g(k * k);
+  int lw = 0;
+  GQ_SOLVER(cusolverDnDpotrf_bufferSize(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, &lw));
+  DevBuf work((int64_t)lw + 1);
+  DevArray<int> info;
+  info.upload(std::vector<int>(2, 0));
+  for (int pass = 0; pass < 2; ++pass) {
+    GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, kk, kk, d, &one, q, d, q, d, &zero, g.p,
+                        kk));
+    GQ_SOLVER(cusolverDnDpotrf(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, work.p, lw,
+                               info.p + pass));
+    GQ_BLAS(cublasDtrsm(bh, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                        CUBLAS_DIAG_NON_UNIT, d, kk, &one, g.p, kk, q, d));
+  }
+  int hinfo[2] = {0, 0};
+  GQ_CUDA(cudaMemcpyAsync(hinfo, info.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  sync();
+  if (hinfo[0] != 0 || hinfo[1] != 0) fail(kSolverError, "CholeskyQR2: Cholesky failed");
+}
+
+// Transposed Gram route for a group whose canonical side has `canon` rows
+// and whose other side has `other`: worth it when the other side is much
+// smaller (eigensolve time grows about as n^1.4 at these sizes on GB300,
+// the extra projection and CholeskyQR2 cost a few GEMMs).
+bool transposed_gram(int64_t canon, int64_t other) {
+  return canon >= 256 && (double)other <= 0.7 * (double)canon;
+}
+
 // Canonical completion: k orthonormal columns orthogonal to the r
 // orthonormal columns of `vecs` (dim x r, col-major, ld dim), written to
 // out (dim x k, col-major, ld dim).  The seed matrix is projected off `vecs`
@@ -248,26 +321,7 @@ void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, int 
                           out, d));
     }
   }
-  auto sh = solver();
-  DevBuf g(k * k);
-  int lw = 0;
-  GQ_SOLVER(cusolverDnDpotrf_bufferSize(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, &lw));
-  DevBuf work((int64_t)lw + 1);
-  DevArray<int> info;
-  info.upload(std::vector<int>(2, 0));
-  for (int pass = 0; pass < 2; ++pass) {
-    GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, kk, kk, d, &one, out, d, out, d, &zero, g.p,
-                        kk));
-    GQ_SOLVER(cusolverDnDpotrf(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, work.p, lw,
-                               info.p + pass));
-    GQ_BLAS(cublasDtrsm(bh, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                        CUBLAS_DIAG_NON_UNIT, d, kk, &one, g.p, kk, out, d));
-  }
-  int hinfo[2] = {0, 0};
-  GQ_CUDA(cudaMemcpyAsync(hinfo, info.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
-  sync();
-  if (hinfo[0] != 0 || hinfo[1] != 0)
-    fail(kSolverError, "null-space completion: Cholesky failed");
+  cholqr2(out, dim, k);
 }
 
 struct Group {
@@ -282,6 +336,7 @@ struct Group {
   int64_t sv_off = 0;             // singular values (small: 32 per group, jacobi: p)
   int64_t ev_off = 0, w_off = 0;  // gram: eigenvectors (dim x dim) and eigenvalues
   int64_t dim = 0;
+  bool eig_m = true;              // gram: eigensolve on Theta Theta^T (else Theta^T Theta)
   int64_t small_idx = -1;
   std::vector<double> svals;      // p values, descending
   std::vector<int> src_cols;      // source column of each value
@@ -290,6 +345,12 @@ struct Group {
   int64_t L_off = 0, R_off = 0;   // outputs: L (m x keep), R (n x keep)
 };
 }  // namespace
+
+void destroy_lane_handles(Lane &l) {
+  if (l.cusolver) cusolverDnDestroy((cusolverDnHandle_t)l.cusolver);
+  if (l.cublas) cublasDestroy((cublasHandle_t)l.cublas);
+  l.cusolver = l.cublas = nullptr;
+}
 
 SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_err,
                     int64_t dmin, int64_t dmax, int scale_side) {
@@ -351,8 +412,10 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       g.small_idx = n_small++;
     } else if (scale_side == 2) {
       g.route = kGramLeft;
+      g.eig_m = !transposed_gram(g.m, g.n);
     } else if (scale_side == 1) {
       g.route = kGramRight;
+      g.eig_m = transposed_gram(g.n, g.m);
     } else {
       g.route = kJacobi;
     }
@@ -453,7 +516,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   std::map<int64_t, std::vector<Group *>> buckets;
   for (Group *g : groups)
     if (g->route == kGramLeft || g->route == kGramRight) {
-      const int64_t real = g->route == kGramLeft ? g->m : g->n;
+      const int64_t real = g->eig_m ? g->m : g->n;
       g->dim = real <= 64 ? (real + 31) / 32 * 32 : (real + 63) / 64 * 64;
       buckets[g->dim].push_back(g);
     }
@@ -472,7 +535,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     std::vector<PadDiagItem> pads;
     for (auto &kv : buckets)
       for (Group *g : kv.second)
-        pads.push_back({g->ev_off, (int)g->dim, (int)(g->route == kGramLeft ? g->m : g->n)});
+        pads.push_back({g->ev_off, (int)g->dim, (int)(g->eig_m ? g->m : g->n)});
     {
       DevArray<PadDiagItem> d;
       d.upload(pads);
@@ -484,7 +547,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       for (Group *g : kv.second) {
         const int m = (int)g->m, n = (int)g->n, bs = (int)g->dim;
         const double *X = mats.p + g->mat_off;  // col-major n x m
-        if (g->route == kGramLeft)  // Theta Theta^T = X^T X (m x m)
+        if (g->eig_m)  // Theta Theta^T = X^T X (m x m)
           GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, X, n, X, n, &zero,
                               ev.p + g->ev_off, bs));
         else  // Theta^T Theta = X X^T (n x n)
@@ -658,10 +721,11 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
           break;
         }
         case kGramLeft:
-          l_ev.push_back({g->ev_off, g->L_off, (int)g->m, (int)g->dim, (int)g->m, sc, (int)j, 1.0});
-          break;
         case kGramRight:
-          r_ev.push_back({g->ev_off, g->R_off, (int)g->n, (int)g->dim, (int)g->n, sc, (int)j, 1.0});
+          if (g->eig_m)
+            l_ev.push_back({g->ev_off, g->L_off, (int)g->m, (int)g->dim, (int)g->m, sc, (int)j, 1.0});
+          else
+            r_ev.push_back({g->ev_off, g->R_off, (int)g->n, (int)g->dim, (int)g->n, sc, (int)j, 1.0});
           break;
       }
     }
@@ -672,19 +736,37 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   launch_items(col_copy_kernel, r_jac, jr.p, Rb.p);
   launch_items(col_copy_kernel, l_ev, ev.p, Lb.p);
   launch_items(col_copy_kernel, r_ev, ev.p, Rb.p);
-  // projections for the Gram routes: R = X L (left) or L = X^T R (right)
+  // projections for the Gram routes: R = X L (canonical left) or L = X^T R
+  // (canonical right); a transposed route first builds the canonical factor
+  // from the other side's eigenvectors (L = qr(X^T R) or R = qr(X L))
   {
     const double one = 1.0, zero = 0.0;
     for (Group *g : groups) {
-      if (g->keep_nz == 0) continue;
+      if (g->keep_nz == 0 || (g->route != kGramLeft && g->route != kGramRight)) continue;
       const int m = (int)g->m, n = (int)g->n, k = (int)g->keep_nz;
       const double *X = mats.p + g->mat_off;
-      if (g->route == kGramLeft)
-        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, &one, X, n, Lb.p + g->L_off, m,
-                            &zero, Rb.p + g->R_off, n));
-      else if (g->route == kGramRight)
-        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, k, n, &one, X, n, Rb.p + g->R_off, n,
-                            &zero, Lb.p + g->L_off, m));
+      double *L = Lb.p + g->L_off, *R = Rb.p + g->R_off;
+      auto left_from_right = [&] {  // L = X^T R (m x k)
+        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, k, n, &one, X, n, R, n, &zero, L, m));
+      };
+      auto right_from_left = [&] {  // R = X L (n x k)
+        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, &one, X, n, L, m, &zero, R, n));
+      };
+      if (g->route == kGramLeft) {
+        if (!g->eig_m) {
+          left_from_right();
+          normalise_columns(L, m, k);
+          cholqr2(L, m, k);
+        }
+        right_from_left();
+      } else {
+        if (g->eig_m) {
+          right_from_left();
+          normalise_columns(R, n, k);
+          cholqr2(R, n, k);
+        }
+        left_from_right();
+      }
     }
   }
   // sign convention on the kept nonzero columns (by the left factor)
@@ -710,6 +792,13 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       DevBuf q(std::max<int64_t>(dim * g->nnz, 1));
       std::vector<ColItem> items;
       const bool gram = g->route == kGramLeft || g->route == kGramRight;
+      if (gram && g->eig_m != left) {
+        // transposed route: every nonzero value is kept (a zero is), so the
+        // canonical factor's first nnz columns are the nonzero vectors
+        null_completion(left ? Lb.p + g->L_off : Rb.p + g->R_off, dim, g->nnz, kz, (int)gi,
+                        left ? 0 : 1, dst);
+        return;
+      }
       for (int64_t j = 0; j < g->nnz; ++j)
         items.push_back({gram ? g->ev_off : (left ? g->lv_off : g->rv_off), 0, (int)dim,
                          gram ? (int)g->dim : (left ? g->ld_l : g->ld_r), (int)dim,

@@ -5,7 +5,9 @@ Mirrors the reference interface
 ``include/gqmps2/algorithm/lanczos_solver.h``):
 
 * ``SweepParams(sweeps, Dmin, Dmax, trunc_err, lancz_params, mps_path="mps",
-  temp_path=".temp")`` plus a keyword ``precision`` ("fp64" | "tf32x3");
+  temp_path=".temp")`` plus the keywords ``precision`` ("fp64" | "tf32x3" |
+  "fp64tc") and ``rayleigh`` ("fp64" | "fp64tc": arithmetic of the split
+  form's Rayleigh-quotient energy);
 * ``LanczosParams(error=1e-7, max_iterations=200)``;
 * ``TwoSiteFiniteVMPS(mps, mpo, sweep_params) -> e0`` with the reference's
   file contract: the MPS is read from ``mps_path`` (``mps.Dump(path, True)``
@@ -31,7 +33,7 @@ from .finite_mps import (FiniteMPS, GenEnvTenName, GenMPSTenName, kMpsPath, kRun
                          read_tensor, write_tensor)
 from .tensor import GQTensor, QN, Div
 
-_PREC = {"fp64": _lib.PREC_FP64, "tf32x3": _lib.PREC_TF32X3}
+_PREC = {"fp64": _lib.PREC_FP64, "tf32x3": _lib.PREC_TF32X3, "fp64tc": _lib.PREC_FP64TC}
 
 
 class LanczosParams:
@@ -43,7 +45,7 @@ class LanczosParams:
 class SweepParams:
     def __init__(self, sweeps, dmin, dmax, trunc_err, lancz_params=None,
                  mps_path: str = kMpsPath, temp_path: str = kRuntimeTempPath,
-                 precision: str = "fp64", verbose: bool = False):
+                 precision: str = "fp64", verbose: bool = False, rayleigh: str = "fp64"):
         self.sweeps = int(sweeps)
         self.Dmin = int(dmin)
         self.Dmax = int(dmax)
@@ -52,14 +54,18 @@ class SweepParams:
         self.mps_path = mps_path
         self.temp_path = temp_path
         if precision not in _PREC:
-            raise ValueError("precision must be 'fp64' or 'tf32x3'")
+            raise ValueError("precision must be 'fp64', 'tf32x3' or 'fp64tc'")
+        if rayleigh not in ("fp64", "fp64tc"):
+            raise ValueError("rayleigh must be 'fp64' or 'fp64tc'")
         self.precision = precision
         self.verbose = bool(verbose)
+        self.rayleigh = rayleigh
 
     def to_c(self, sweeps: Optional[int] = None) -> _lib.SweepParamsC:
         return _lib.SweepParamsC(
             self.sweeps if sweeps is None else sweeps, self.Dmin, self.Dmax, self.trunc_err,
-            _lib.LanczosParamsC(self.lancz_params.error, self.lancz_params.max_iterations),
+            _lib.LanczosParamsC(self.lancz_params.error, self.lancz_params.max_iterations,
+                                _PREC[self.rayleigh]),
             _PREC[self.precision], 1 if self.verbose else 0)
 
 
@@ -76,6 +82,23 @@ class UpdateStats:
         return (f"Site {self.site:4d} E0 = {self.e0:20.16f} TruncErr = {self.trunc_err:.2e} "
                 f"D = {self.D:5d} Iter = {self.iters:3d} LanczT = {self.lanczos_seconds:8.3f} "
                 f"TotT = {self.update_seconds:8.3f} S = {self.ee:10.7f}")
+
+
+def run_batch(states: Sequence["DMRGState"], params: Sequence[SweepParams],
+              init_envs: bool = True, nthreads: int = 8) -> List[float]:
+    """Sweep independent DMRG states concurrently (``gq_dmrg_run_batch``):
+    host threads with one CUDA stream each take the states in order; each
+    state builds its right environments (if ``init_envs``) and runs its own
+    ``params[i].sweeps`` sweeps.  Returns each state's last energy."""
+    n = len(states)
+    if len(params) != n:
+        raise ValueError("one SweepParams per state")
+    hs = (C.c_void_p * max(n, 1))(*[s.h.value for s in states])
+    ps = (_lib.SweepParamsC * max(n, 1))(*[p.to_c() for p in params])
+    e0 = np.zeros(max(n, 1))
+    check(load().gq_dmrg_run_batch(hs, n, ps, 1 if init_envs else 0, int(nthreads),
+                                   e0.ctypes.data_as(_lib._DP)))
+    return [float(x) for x in e0[:n]]
 
 
 class DMRGState:
@@ -199,15 +222,18 @@ def _dev(t: Optional[GQTensor]):
 
 
 def LanczosSolver(eff_ham: Sequence[Optional[GQTensor]], init_state: GQTensor,
-                  params: LanczosParams, where: str, precision: str = "fp64") -> LanczosRes:
+                  params: LanczosParams, where: str, precision: str = "fp64",
+                  rayleigh: str = "fp64") -> LanczosRes:
     """``LanczosSolver`` (``lanczos_solver_impl.h:79-226``); ``eff_ham`` is
-    ``[L, W_l, W_r, R]`` with ``L``/``R`` ``None`` at the chain ends."""
+    ``[L, W_l, W_r, R]`` with ``L``/``R`` ``None`` at the chain ends.
+    ``rayleigh`` ("fp64" | "fp64tc"): arithmetic of the split form's
+    Rayleigh-quotient energy."""
     lib = load()
     L, Wl, Wr, R = [_dev(t) for t in eff_ham]
     x = DeviceTensor.from_host(init_state)
     it, e = C.c_int64(), C.c_double()
     out = C.c_void_p()
-    lp = _lib.LanczosParamsC(params.error, params.max_iterations)
+    lp = _lib.LanczosParamsC(params.error, params.max_iterations, _PREC[rayleigh])
     check(lib.gq_lanczos(L.h if L else None, Wl.h, Wr.h, R.h if R else None, _lib.WHERE[where],
                          x.h, C.byref(lp), _PREC[precision], C.byref(it), C.byref(e),
                          C.byref(out)))

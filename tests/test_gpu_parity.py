@@ -13,7 +13,7 @@ from oracle.lanczos import LanczosParams as OLP, MATVEC
 from oracle.vmps import SweepParams as OSP
 from mps2_gb300 import hamiltonians as H
 from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS
-from mps2_gb300.tensor import GQTensor, IN, OUT
+from mps2_gb300.tensor import GQTensor, IN, Index, OUT
 from _convert import from_oracle, to_oracle
 from _helpers import first_allowed_div, oracle_state, random_index, random_tensor, rel_err
 from golden_cases import cases
@@ -185,6 +185,47 @@ def test_svd_zero_completion_matches_oracle(lib):
     np.testing.assert_allclose(s, ref.svals, rtol=1e-12, atol=1e-14)
     assert rel_err(u, ref.u) <= 1e-9
     assert rel_err(vt, ref.vt) <= 1e-9
+
+
+def _scale_leg(t, leg, s):
+    """t with its slices along `leg` (sectors in index order, flattened)
+    multiplied by the values s."""
+    out = t.copy()
+    offs = np.cumsum([0] + [d for _, d in t.indices[leg].sectors()])
+    for k in out.blocks:
+        sh = [1] * out.blocks[k].ndim
+        sh[leg] = -1
+        out.blocks[k] = out.blocks[k] * s[offs[k[leg]]:offs[k[leg] + 1]].reshape(sh)
+    return out
+
+
+@pytest.mark.parametrize("scale_side", [1, 2])
+@pytest.mark.parametrize("big_side", ["l", "r"])
+def test_svd_gram_routes_match_oracle(lib, scale_side, big_side):
+    """Groups of a few hundred rows on one side: the sweep's Gram routes
+    ('r': U orthonormal, S.Vt returned; 'l': V orthonormal, U.S returned),
+    on the canonical side's Gram matrix or -- when the other side is much
+    smaller -- on the other side's, against the oracle's SVD."""
+    from mps2_gb300.vmps import SVD
+    rng = np.random.default_rng(17 + scale_side)
+    big = Index([((-1,), 300), ((1,), 280)], IN)
+    small = Index([((-1,), 60), ((1,), 70)], IN)
+    l = big if big_side == "l" else small
+    r = (small if big_side == "l" else big).inverse()
+    s1 = Index([((1,), 1), ((-1,), 1)], OUT)
+    s2 = Index([((1,), 1), ((-1,), 1)], OUT)
+    t = random_tensor(rng, [l, s1, s2, r], (0,))
+    ref = oracle.svd(to_oracle(t), 2, (0,), 0.0, 1, 150)
+    u, s, vt, err, D = SVD(t, 2, (0,), 0.0, 1, 150, scale_side=scale_side)
+    assert D == ref.D
+    np.testing.assert_allclose(s, ref.svals, rtol=1e-10)
+    ru, rvt = from_oracle(ref.u), from_oracle(ref.vt)
+    if scale_side == 2:
+        rvt = _scale_leg(rvt, 0, np.asarray(ref.svals))
+    else:
+        ru = _scale_leg(ru, 2, np.asarray(ref.svals))
+    assert rel_err(u, to_oracle(ru)) <= 1e-9
+    assert rel_err(vt, to_oracle(rvt)) <= 1e-9
 
 
 # --------------------------------------------------------------------------
