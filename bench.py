@@ -62,6 +62,11 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--record-structure", action="store_true",
                    help="write the central-bond block structure fixture")
+    p.add_argument("--workload", choices=["sweep", "batched"], default="sweep",
+                   help="sweep: the D=2000 chain (headline); batched: 64 independent XXZ "
+                        "chains, concurrent vs one after another")
+    p.add_argument("--instances", type=int, default=64)
+    p.add_argument("--threads", type=int, default=16)
     return p.parse_args()
 
 
@@ -318,6 +323,7 @@ def run_ours(args):
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     prof = {k: profile_read(k) for k in FAMILIES}
+    svd_span = {k: profile_read(k) for k in ("svd", "svd_eig")}
     profile_enable(False)
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
@@ -428,7 +434,9 @@ def run_ours(args):
         "energy_last_sweep": energies[-1],
         "gpu_launches": int(n_launch_ours),
         "time_split_s": {"lanczos": tot["lanczos_seconds"], "svd": tot["svd_seconds"],
-                         "env": tot["env_seconds"], "matvecs": tot["matvecs"]},
+                         "env": tot["env_seconds"], "matvecs": tot["matvecs"],
+                         "svd_device_span": svd_span["svd"][1] * 1e-3,
+                         "svd_decompositions": svd_span["svd_eig"][1] * 1e-3},
         "central_problem": {"fp64": solve["fp64"], "tf32x3": solve["tf32x3"],
                             "delta_e_rel": de,
                             "fp64_sweep_s_est": sweep_s * u64 / gpu_center.update_seconds},
@@ -448,9 +456,97 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# Batched independent instances
+# ---------------------------------------------------------------------------
+def batched_instances(n, seed=5):
+    """n XXZ open chains, seeded: L uniform in [16, 64] (even, so the Neel
+    state has Sz=0), Delta uniform in [0.5, 1.5], D in {64, 128, 256, 512}."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        L = int(rng.integers(8, 33)) * 2
+        delta = float(rng.uniform(0.5, 1.5))
+        D = int(rng.choice([64, 128, 256, 512]))
+        out.append((L, delta, D))
+    return out
+
+
+def run_batched(args):
+    """One step = every instance swept 4 times from its Neel product state,
+    split form; timed one after another on one stream and concurrently
+    (host threads with one stream each).  The metric is instances per
+    second of the concurrent run; the serial run and the energy agreement
+    between the two are reported beside it."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    from mps2_gb300 import _lib
+    from mps2_gb300 import hamiltonians as H
+    from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS
+    from mps2_gb300.vmps import DMRGState, LanczosParams, SweepParams, run_batch
+    _lib.check(_lib.load().gq_init(0))
+    cases = batched_instances(args.instances)
+    built = []
+    for L, delta, D in cases:
+        sv, mpo, qn0, _ = H.heisenberg_chain(L, 1.0, delta)
+        mps = FiniteMPS(sv)
+        DirectStateInitMps(mps, H.neel_shuffled_labels(L, L), qn0)
+        built.append((mps.tens, mpo))
+    params = [SweepParams(4, D, D, 0.0, LanczosParams(1e-9, 100), precision=args.precision,
+                          rayleigh=args.rayleigh) for _, _, D in cases]
+
+    def serial():
+        es = []
+        for (tens, mpo), p in zip(built, params):
+            st = DMRGState(tens, mpo)
+            st.init_envs(p.precision)
+            es.append(st.sweep(p)[0])
+        return es
+
+    def concurrent():
+        states = [DMRGState(tens, mpo) for tens, mpo in built]
+        return run_batch(states, params, init_envs=True, nthreads=args.threads)
+
+    for _ in range(args.warmup):
+        concurrent()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e_conc = concurrent()
+    torch.cuda.synchronize()
+    t_conc = (time.perf_counter() - t0) / args.steps
+    t0 = time.perf_counter()
+    e_ser = serial()
+    torch.cuda.synchronize()
+    t_ser = time.perf_counter() - t0
+    dev = max(abs(a - b) / abs(b) for a, b in zip(e_conc, e_ser))
+    line = {
+        "metric": "batched XXZ instances, 4 sweeps each (instances/s)",
+        "value": len(cases) / t_conc, "unit": "instances/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_conc * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else args.precision,
+        "data": "synthetic models (seeded XXZ chains), no dataset",
+        "config": {"workload": f"xxz_batch_{len(cases)}", "instances": len(cases),
+                   "threads": args.threads, "precision": args.precision,
+                   "L_range": [min(c[0] for c in cases), max(c[0] for c in cases)],
+                   "D_set": sorted(set(c[2] for c in cases)), "sweeps": 4},
+        "serial_seconds": t_ser, "concurrent_seconds": t_conc,
+        "speedup_over_serial": t_ser / t_conc,
+        "max_rel_energy_diff_concurrent_vs_serial": dev,
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = _args()
-    if args.impl == "reference":
+    if args.workload == "batched":
+        # one hardware queue per concurrent stream (must precede CUDA init)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+        run_batched(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -231,6 +231,8 @@ int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *para
 #define GQ_PROF_VECTOR 3
 #define GQ_PROF_SKINNY 4
 #define GQ_PROF_GEMM_FP64TC 5
+#define GQ_PROF_SVD 6     /* whole SVD, device span including library calls */
+#define GQ_PROF_SVD_EIG 7 /* its decompositions */
 int gq_profile_enable(int on);
 int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes);
 /* The cudaStream_t all library work is queued on. */

@@ -48,7 +48,9 @@ enum ProfKernel : int {
   kProfVector = 3,     // Lanczos vector kernels
   kProfSkinny = 4,     // tall-skinny MPO-tensor contractions
   kProfGemmFp64Tc = 5, // FP64-accurate exact-slice tcgen05 grouped GEMM
-  kProfCount = 6,
+  kProfSvd = 6,        // whole truncating SVD (device span, library calls included)
+  kProfSvdEig = 7,     // its decompositions (cuSOLVER eigensolves / Jacobi, Gram GEMMs)
+  kProfCount = 8,
 };
 bool prof_on();
 void prof_enable(bool on);

@@ -354,6 +354,7 @@ void destroy_lane_handles(Lane &l) {
 
 SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_err,
                     int64_t dmin, int64_t dmax, int scale_side) {
+  prof_begin(kProfSvd);
   // Every allowed block takes part; embed a sparser tensor first.
   TensorPtr full;
   if ((size_t)t_in.nblocks() != allowed_blocks(t_in.idx, t_in.div).size()) {
@@ -439,6 +440,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   }
 
   // ---- decompositions -----------------------------------------------------
+  prof_begin(kProfSvdEig);
   auto h = solver();
   auto bh = blas();
   gesvdjInfo_t prm;
@@ -581,6 +583,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     }
     cusolverDnDestroyParams(sp);
   }
+  prof_end(kProfSvdEig, 0.0, 0.0);
   // ---- values to the host ---------------------------------------------------
   std::vector<double> hs_small(n_small * kSmall), hs_j(js_total), hw(w_total);
   std::vector<int> hinfo_s(n_small), hinfo_j(groups.size(), 0), hinfo_e(n_gram, 0);
@@ -870,6 +873,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
                                                          out.vt->data.p);
     GQ_CUDA(cudaGetLastError());
   }
+  prof_end(kProfSvd, 0.0, 0.0);
   return out;
 }
 
