@@ -209,6 +209,21 @@ int gq_dmrg_update(gq_dmrg *d, const gq_sweep_params *params, int dir, int targe
 int gq_dmrg_get_mps(gq_dmrg *d, int i, gq_tensor **out);
 int gq_dmrg_destroy(gq_dmrg *d);
 
+/* Finite-MPS canonicalisation ---------------------------------------------- *
+ * FiniteMPS::Centralize (one_dim_tn/mps/finite_mps/finite_mps.h:149-248) and
+ * TruncateMPS (:251-300) on device tensors, in place: the n handles of `mps`
+ * (site order, the reference's leg orders) are rewritten.  `cano` holds the
+ * canonical type of each site (GQ_CANO_*), read and updated as the
+ * reference's tens_cano_type_ is. */
+#define GQ_CANO_NONE 0
+#define GQ_CANO_LEFT 1
+#define GQ_CANO_RIGHT 2
+int gq_mps_centralize(gq_tensor *const *mps, int n, int center, int *cano);
+/* errs[n-1], Ds[n-1] (optional): truncation error and bond dimension of each
+ * bond (the reference prints them). */
+int gq_mps_truncate(gq_tensor *const *mps, int n, int *cano, double trunc_err, int64_t dmin,
+                    int64_t dmax, double *errs, int64_t *Ds);
+
 /* Batched instances ------------------------------------------------------ *
  * Not in the reference (its tests run one chain per process).  Runs n
  * independent DMRG states concurrently: a pool of `nthreads` host threads,

@@ -363,6 +363,52 @@ int gq_dmrg_sweep(gq_dmrg *d, const gq_sweep_params *p, gq_update_stats *stats, 
   });
 }
 
+namespace {
+std::vector<gq::TensorPtr> mps_of(gq_tensor *const *mps, int n) {
+  GQ_CHECK(mps && n >= 2, "an MPS needs at least two sites");
+  std::vector<gq::TensorPtr> v(n);
+  for (int i = 0; i < n; ++i) {
+    GQ_CHECK(mps[i] && mps[i]->t, "null MPS tensor");
+    v[i] = mps[i]->t;
+  }
+  return v;
+}
+}  // namespace
+
+int gq_mps_centralize(gq_tensor *const *mps, int n, int center, int *cano) {
+  return guarded([&] {
+    auto v = mps_of(mps, n);
+    GQ_CHECK(cano, "null canonical-type array");
+    std::vector<int> c(cano, cano + n);
+    gq::centralize(v, c, center);
+    gq::sync();
+    for (int i = 0; i < n; ++i) {
+      mps[i]->t = v[i];
+      cano[i] = c[i];
+    }
+  });
+}
+
+int gq_mps_truncate(gq_tensor *const *mps, int n, int *cano, double trunc_err, int64_t dmin,
+                    int64_t dmax, double *errs, int64_t *Ds) {
+  return guarded([&] {
+    auto v = mps_of(mps, n);
+    GQ_CHECK(cano, "null canonical-type array");
+    GQ_CHECK(dmin >= 1 && dmax >= dmin, "bad Dmin/Dmax");
+    std::vector<int> c(cano, cano + n);
+    auto res = gq::truncate_mps(v, c, trunc_err, dmin, dmax);
+    gq::sync();
+    for (int i = 0; i < n; ++i) {
+      mps[i]->t = v[i];
+      cano[i] = c[i];
+    }
+    for (size_t b = 0; b < res.size(); ++b) {
+      if (errs) errs[b] = res[b].first;
+      if (Ds) Ds[b] = res[b].second;
+    }
+  });
+}
+
 int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *params,
                       int init_envs, int nthreads, double *e0) {
   return guarded([&] {

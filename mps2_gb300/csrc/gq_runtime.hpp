@@ -274,6 +274,18 @@ SvdOut svd_truncate(const Tensor &t, int ldims, const QN &ldiv, double trunc_err
 bool tridiag_lowest(const double *a, const double *b, int n, double *eval, double *vec);
 
 // ---------------------------------------------------------------------------
+// Finite-MPS canonicalisation and truncation (mps.cu)
+// ---------------------------------------------------------------------------
+enum CanoType : int { kCanoNone = 0, kCanoLeft = 1, kCanoRight = 2 };
+void left_canonicalize_ten(std::vector<TensorPtr> &mps, std::vector<int> &cano, int i);
+void right_canonicalize_ten(std::vector<TensorPtr> &mps, std::vector<int> &cano, int i);
+void centralize(std::vector<TensorPtr> &mps, std::vector<int> &cano, int center);
+// (truncation error, D) per bond
+std::vector<std::pair<double, int64_t>> truncate_mps(std::vector<TensorPtr> &mps,
+                                                     std::vector<int> &cano, double trunc_err,
+                                                     int64_t dmin, int64_t dmax);
+
+// ---------------------------------------------------------------------------
 // Effective Hamiltonian and Lanczos (lanczos.cu)
 // ---------------------------------------------------------------------------
 enum Where : int { kLend = 0, kCent = 1, kRend = 2 };

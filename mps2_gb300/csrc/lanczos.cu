@@ -9,6 +9,7 @@
 // and replayed every iteration.
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 
 #include "gq_runtime.hpp"
 
@@ -28,7 +29,54 @@ struct MatvecPlan {
   std::vector<TensorPtr> inter;
   DevBuf scratch;
   double flops = 0.0;
+  // The matvec's launch sequence is fixed for a whole Lanczos solve, so it
+  // is captured once as a CUDA graph reading a fixed input buffer and
+  // replayed every iteration (captured lazily, for one (x, y) pair).
+  cudaGraphExec_t exec = nullptr;
+  const double *graph_x = nullptr;
+  double *graph_y = nullptr;
+  ~MatvecPlan() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
 };
+
+namespace {
+// Graph replay of the matvec, unless the kernel profiler is on (it times
+// every launch with its own events) or GQ_NO_GRAPHS is set.
+bool graphs_enabled() {
+  static const bool off = std::getenv("GQ_NO_GRAPHS") != nullptr;
+  return !off && !prof_on();
+}
+
+void run_matvec_graph(MatvecPlan &p, const double *x, double *y, double *xin, int64_t n) {
+  auto s = stream();
+  if (!p.exec || p.graph_x != xin || p.graph_y != y) {
+    if (p.exec) {
+      GQ_CUDA(cudaGraphExecDestroy(p.exec));
+      p.exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    GQ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      run_matvec(p, xin, y);
+    } catch (...) {
+      cudaGraph_t dead = nullptr;
+      cudaStreamEndCapture(s, &dead);
+      if (dead) cudaGraphDestroy(dead);
+      throw;
+    }
+    GQ_CUDA(cudaStreamEndCapture(s, &g));
+    const cudaError_t e = cudaGraphInstantiate(&p.exec, g, 0);
+    cudaGraphDestroy(g);
+    GQ_CUDA(e);
+    p.graph_x = xin;
+    p.graph_y = y;
+  }
+  if (x != xin)
+    GQ_CUDA(cudaMemcpyAsync(xin, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  GQ_CUDA(cudaGraphLaunch(p.exec, s));
+}
+}  // namespace
 
 int64_t eff_ham_dim(const EffHam &h) {
   switch (h.where) {
@@ -160,9 +208,14 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   DevBuf red(dot_scratch_elems());
   std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
   double *hs = lane().host_scalars;
+  const bool use_graph = graphs_enabled();
+  DevBuf xin(use_graph ? n : 0);
 
   auto matvec = [&](const double *x) {
-    run_matvec(*plan, x, last.p);
+    if (use_graph)
+      run_matvec_graph(*plan, x, last.p, xin.p, n);
+    else
+      run_matvec(*plan, x, last.p);
     res.matvecs++;
     res.matvec_flops += plan->flops;
   };

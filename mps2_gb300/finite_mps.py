@@ -110,10 +110,28 @@ def read_tensor(path: str) -> GQTensor:
 class FiniteMPS:
     """A finite MPS: ``N`` optional site tensors plus the site information."""
 
+    # canonical types of the site tensors (``MPSTenCanoType``)
+    NONE, LEFT, RIGHT = 0, 1, 2
+
     def __init__(self, site_vec: SiteVec):
         self.site_vec = site_vec
         self.tens: List[Optional[GQTensor]] = [None] * site_vec.size
         self.center = None
+        self.tens_cano_type = [FiniteMPS.NONE] * site_vec.size
+
+    def GetCenter(self):
+        return self.center
+
+    def GetTensCanoType(self) -> List[int]:
+        return list(self.tens_cano_type)
+
+    def Centralize(self, target_center: int) -> None:
+        """``FiniteMPS::Centralize`` (``finite_mps.h:149-248``) on the GPU:
+        the site tensors are uploaded, canonicalised by device SVDs and
+        contractions, and downloaded again."""
+        from .vmps import mps_centralize
+        mps_centralize(self, target_center)
+        self.center = target_center
 
     def size(self) -> int:
         return len(self.tens)
@@ -186,3 +204,4 @@ def DirectStateInitMps(mps: FiniteMPS, stat_labs: Sequence[int], zero_div) -> No
     t[0, stat_labs[N - 1]] = 1.0
     mps[N - 1] = t
     mps.center = 0
+    mps.tens_cano_type = [FiniteMPS.NONE] + [FiniteMPS.RIGHT] * (N - 1)

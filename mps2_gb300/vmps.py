@@ -281,3 +281,39 @@ def SVD(t: GQTensor, ldims: int, ldiv, trunc_err: float, dmin: int, dmax: int,
                      C.byref(D)))
     return (DeviceTensor(u.value).to_host(), s[:D.value].copy(), DeviceTensor(vt.value).to_host(),
             err.value, D.value)
+
+
+# ---------------------------------------------------------------------------
+# Finite-MPS canonicalisation and truncation (device)
+# ---------------------------------------------------------------------------
+def _mps_handles(mps: FiniteMPS):
+    dev = [DeviceTensor.from_host(mps[i]) for i in range(mps.size())]
+    arr = (C.c_void_p * len(dev))(*[t.h.value for t in dev])
+    cano = (C.c_int * len(dev))(*mps.tens_cano_type)
+    return dev, arr, cano
+
+
+def mps_centralize(mps: FiniteMPS, center: int) -> None:
+    """Backs ``FiniteMPS.Centralize`` (``gq_mps_centralize``)."""
+    dev, arr, cano = _mps_handles(mps)
+    check(load().gq_mps_centralize(arr, len(dev), int(center), cano))
+    for i, t in enumerate(dev):
+        mps[i] = t.to_host()
+    mps.tens_cano_type = list(cano)
+
+
+def TruncateMPS(mps: FiniteMPS, trunc_err: float, Dmin: int, Dmax: int):
+    """``TruncateMPS`` (``finite_mps.h:251-300``) on the GPU.  Returns the
+    (truncation error, D) of every bond, which the reference prints."""
+    dev, arr, cano = _mps_handles(mps)
+    n = len(dev)
+    errs = np.zeros(max(n - 1, 1))
+    Ds = np.zeros(max(n - 1, 1), dtype=np.int64)
+    check(load().gq_mps_truncate(arr, n, cano, float(trunc_err), int(Dmin), int(Dmax),
+                                 errs.ctypes.data_as(_lib._DP),
+                                 Ds.ctypes.data_as(C.POINTER(C.c_int64))))
+    for i, t in enumerate(dev):
+        mps[i] = t.to_host()
+    mps.tens_cano_type = list(cano)
+    mps.center = None
+    return [(float(e), int(d)) for e, d in zip(errs[:n - 1], Ds[:n - 1])]

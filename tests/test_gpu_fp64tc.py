@@ -156,17 +156,18 @@ def test_sweeps_in_fp64tc_and_split_forms_match_fp64(lib):
 
 def test_fp64tc_lanczos_energy_matches_fp64_same_problem(lib):
     """The reference's Lanczos set-up (``test_lanczos_solver.cc:121-153``:
-    symmetric environments, one sector per leg) at D=256, 30 iterations:
-    the FP64-accurate tensor-core Lanczos tracks the FP64 one's energy to
-    1e-11 relative."""
+    symmetric environments, one sector per leg) at D=256, 7 Lanczos steps
+    (an unconverged Krylov space of a random operator amplifies rounding
+    differences with every further step): the FP64-accurate tensor-core
+    Lanczos tracks the FP64 one's energy to 1e-12 relative."""
     from mps2_gb300.vmps import LanczosParams, LanczosSolver
     from test_oracle_golden import _random_sym_env
     rng = np.random.default_rng(3)
     eff, theta = _random_sym_env(rng, 256, 2, 2)
     eff = [from_oracle(t) for t in eff]
     theta = from_oracle(theta)
-    lp = LanczosParams(1e-15, 30)
+    lp = LanczosParams(1e-15, 8)
     e64 = LanczosSolver(eff, theta, lp, "cent", precision="fp64").gs_eng
     res, n = oz_launches(lambda: LanczosSolver(eff, theta, lp, "cent", precision="fp64tc"))
     assert n > 0, "the tensor-core kernel did not run"
-    assert abs(res.gs_eng - e64) / abs(e64) <= 1e-11, (res.gs_eng, e64)
+    assert abs(res.gs_eng - e64) / abs(e64) <= 1e-12, (res.gs_eng, e64)

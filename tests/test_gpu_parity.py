@@ -133,6 +133,27 @@ def test_lanczos_matches_oracle(lib, where):
     assert rel_err(a * s, ref.gs_vec) <= 1e-6
 
 
+@pytest.mark.parametrize("prec", ["fp64", "tf32x3"])
+def test_lanczos_graph_replay_matches_launch_by_launch(lib, prec):
+    """The matvec replayed as a CUDA graph (default) and launched kernel by
+    kernel (what the kernel profiler forces) run the same kernels in the
+    same order: identical energies and ground states."""
+    from mps2_gb300.vmps import LanczosParams, LanczosSolver, profile_enable
+    from test_oracle_golden import _random_sym_env
+    rng = np.random.default_rng(8)
+    eff, theta = _random_sym_env(rng, 160, 2, 2)
+    eff = [from_oracle(t) for t in eff]
+    theta = from_oracle(theta)
+    lp = LanczosParams(1e-12, 40)
+    a = LanczosSolver(eff, theta, lp, "cent", precision=prec)
+    profile_enable(True)
+    b = LanczosSolver(eff, theta, lp, "cent", precision=prec)
+    profile_enable(False)
+    assert a.iters == b.iters
+    assert a.gs_eng == b.gs_eng
+    assert rel_err(a.gs_vec, to_oracle(b.gs_vec)) == 0.0
+
+
 def test_lanczos_vs_dense_diagonalisation(lib):
     """The reference's Lanczos unit test (``test_lanczos_solver.cc:111``)
     through the GPU solver."""
