@@ -131,6 +131,9 @@ int gq_tensor_describe(const gq_tensor *t, int *rank, int *nq, int64_t *nsec_tot
 int gq_tensor_export(const gq_tensor *t, int *dirs, int *nsecs, int *qns, int64_t *dims,
                      int *div, int *coords, double *data);
 int gq_tensor_destroy(gq_tensor *t);
+/* gqten Dag for real tensors: every leg's direction inverted, divergence
+ * negated, data copied (new handle). */
+int gq_tensor_dag(const gq_tensor *t, gq_tensor **out);
 
 /* Contraction ------------------------------------------------------------ *
  * gqten Contract(a, b, {axes_a, axes_b}, &c): output legs are a's free

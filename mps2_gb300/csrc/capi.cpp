@@ -181,6 +181,13 @@ int gq_tensor_destroy(gq_tensor *h) {
   return guarded([&] { delete h; });
 }
 
+int gq_tensor_dag(const gq_tensor *t, gq_tensor **out) {
+  return guarded([&] {
+    GQ_CHECK(out, "null output");
+    *out = wrap(gq::dag(deref(t, "t")));
+  });
+}
+
 int gq_contract(const gq_tensor *a, const gq_tensor *b, int naxes, const int *axes_a,
                 const int *axes_b, int precision, gq_tensor **out, double *flops) {
   return guarded([&] {
