@@ -479,7 +479,11 @@ def run_ours(args):
                          "svd_device_span": svd_span["svd"][1] * 1e-3,
                          "svd_decompositions": svd_span["svd_eig"][1] * 1e-3},
         "central_problem": {"fp64": solve["fp64"], "tf32x3": solve["tf32x3"],
+                            "fp64tc": solve["fp64tc"],
                             "delta_e_rel": de,
+                            "delta_e_rel_fp64tc": abs(solve["fp64tc"]["energy"] -
+                                                      solve["fp64"]["energy"]) /
+                            abs(solve["fp64"]["energy"]),
                             "fp64_sweep_s_est": sweep_s * u64 / gpu_center.update_seconds},
         "kernels": kernels,
         "roofline": {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak,

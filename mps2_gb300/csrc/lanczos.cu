@@ -31,7 +31,7 @@ struct MatvecPlan {
   double flops = 0.0;
   // The matvec's launch sequence is fixed for a whole Lanczos solve, so it
   // is captured once as a CUDA graph reading a fixed input buffer and
-  // replayed every iteration (captured lazily, for one (x, y) pair).
+  // replayed every further iteration (captured lazily, for one (x, y) pair).
   cudaGraphExec_t exec = nullptr;
   const double *graph_x = nullptr;
   double *graph_y = nullptr;
@@ -211,8 +211,11 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   const bool use_graph = graphs_enabled();
   DevBuf xin(use_graph ? n : 0);
 
+  // A solve that converges within two matvecs (the common case once a
+  // sweep has converged) never pays for capturing and instantiating the
+  // graph; longer solves replay it from the third matvec on.
   auto matvec = [&](const double *x) {
-    if (use_graph)
+    if (use_graph && res.matvecs >= 2)
       run_matvec_graph(*plan, x, last.p, xin.p, n);
     else
       run_matvec(*plan, x, last.p);

@@ -288,6 +288,40 @@ void cholqr2(double *q, int64_t dim, int64_t k) {
   if (hinfo[0] != 0 || hinfo[1] != 0) fail(kSolverError, "CholeskyQR2: Cholesky failed");
 }
 
+// Dense FP64 products of the large groups on the FP64-accurate tensor-core
+// path: A (a0 x a1) and B (b0 x b1) row-major, contracted over A's axis
+// `axa` and B's axis `axb`; C (the two free dimensions, A's first) written
+// row-major.  Each operand is a one-block two-leg tensor (trivial charges)
+// and goes through the block contraction engine; below ~1e8 flops cuBLAS
+// is used instead (kTcMinFlops).
+constexpr double kTcMinFlops = 1e8;
+
+TensorPtr dense_tensor(const double *src, int64_t d0, int64_t d1, int dir0, int dir1) {
+  Index i0, i1;
+  i0.dir = dir0;
+  i0.qn = {QN()};
+  i0.dim = {d0};
+  i1.dir = dir1;
+  i1.qn = {QN()};
+  i1.dim = {d1};
+  auto t = make_structure(1, {i0, i1}, QN(), {{0, 0}});
+  t->allocate();
+  GQ_CUDA(cudaMemcpyAsync(t->data.p, src, sizeof(double) * d0 * d1, cudaMemcpyDeviceToDevice,
+                          stream()));
+  return t;
+}
+
+// C = contraction of A's axis axa with B's axis axb; the contracted pair
+// is given opposite directions, every block is charge-allowed.
+void dense_contract_tc(const double *A, int64_t a0, int64_t a1, int axa, const double *B,
+                       int64_t b0, int64_t b1, int axb, double *C) {
+  auto ta = dense_tensor(A, a0, a1, axa == 0 ? -1 : 1, axa == 1 ? -1 : 1);
+  auto tb = dense_tensor(B, b0, b1, axb == 0 ? 1 : -1, axb == 1 ? 1 : -1);
+  auto tc = contract(*ta, *tb, {axa}, {axb}, kFP64TC);
+  GQ_CUDA(cudaMemcpyAsync(C, tc->data.p, sizeof(double) * tc->size(), cudaMemcpyDeviceToDevice,
+                          stream()));
+}
+
 // Transposed Gram route for a group whose canonical side has `canon` rows
 // and whose other side has `other`: worth it when the other side is much
 // smaller (eigensolve time grows about as n^1.4 at these sizes on GB300,
@@ -549,12 +583,23 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       for (Group *g : kv.second) {
         const int m = (int)g->m, n = (int)g->n, bs = (int)g->dim;
         const double *X = mats.p + g->mat_off;  // col-major n x m
-        if (g->eig_m)  // Theta Theta^T = X^T X (m x m)
+        const int gd = g->eig_m ? m : n;  // Gram dimension
+        if (2.0 * gd * gd * (double)(g->eig_m ? n : m) >= kTcMinFlops) {
+          // X is Theta row-major (m x n): Theta Theta^T contracts axis 1,
+          // Theta^T Theta axis 0; the symmetric result lands in the slot
+          DevBuf gm((int64_t)gd * gd);
+          const int ax = g->eig_m ? 1 : 0;
+          dense_contract_tc(X, m, n, ax, X, m, n, ax, gm.p);
+          GQ_CUDA(cudaMemcpy2DAsync(ev.p + g->ev_off, sizeof(double) * bs, gm.p,
+                                    sizeof(double) * gd, sizeof(double) * gd, gd,
+                                    cudaMemcpyDeviceToDevice, s));
+        } else if (g->eig_m) {  // Theta Theta^T = X^T X (m x m)
           GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, X, n, X, n, &zero,
                               ev.p + g->ev_off, bs));
-        else  // Theta^T Theta = X X^T (n x n)
+        } else {  // Theta^T Theta = X X^T (n x n)
           GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_T, n, n, m, &one, X, n, X, n, &zero,
                               ev.p + g->ev_off, bs));
+        }
       }
     cusolverDnParams_t sp;
     GQ_SOLVER(cusolverDnCreateParams(&sp));
@@ -749,11 +794,21 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       const int m = (int)g->m, n = (int)g->n, k = (int)g->keep_nz;
       const double *X = mats.p + g->mat_off;
       double *L = Lb.p + g->L_off, *R = Rb.p + g->R_off;
-      auto left_from_right = [&] {  // L = X^T R (m x k)
-        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, k, n, &one, X, n, R, n, &zero, L, m));
+      const bool tc = 2.0 * m * n * (double)k >= kTcMinFlops;
+      // L, R col-major (ld m, n) = row-major k x m, k x n
+      auto left_from_right = [&] {  // L = X^T R (m x k): Lrow = Rrow . Theta^T
+        if (tc)
+          dense_contract_tc(R, k, n, 1, X, m, n, 1, L);
+        else
+          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, k, n, &one, X, n, R, n, &zero, L,
+                              m));
       };
-      auto right_from_left = [&] {  // R = X L (n x k)
-        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, &one, X, n, L, m, &zero, R, n));
+      auto right_from_left = [&] {  // R = X L (n x k): Rrow = Lrow . Theta
+        if (tc)
+          dense_contract_tc(L, k, m, 1, X, m, n, 0, R);
+        else
+          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, &one, X, n, L, m, &zero, R,
+                              n));
       };
       if (g->route == kGramLeft) {
         if (!g->eig_m) {

@@ -154,6 +154,26 @@ def test_sweeps_in_fp64tc_and_split_forms_match_fp64(lib):
     assert abs(energies["tf32x3"][-1] - energies["fp64"][-1]) / abs(energies["fp64"][-1]) <= 1e-9
 
 
+def test_fp64tc_matvec_on_symmetric_single_sector_problem(lib):
+    """The reference's Lanczos set-up (one sector per leg, D=256: dense
+    256 x 512 blocks, k up to 512): the FP64-accurate tensor-core matvec
+    against the FP64 one and the oracle."""
+    from mps2_gb300.vmps import eff_ham_mul_state
+    from test_oracle_golden import _random_sym_env
+    rng = np.random.default_rng(3)
+    eff, theta = _random_sym_env(rng, 256, 2, 2)
+    ref = MATVEC["cent"](eff, theta)
+    effg = [from_oracle(t) for t in eff]
+    th = from_oracle(theta)
+    (got64, _), _ = oz_launches(lambda: eff_ham_mul_state(effg, th, "cent", "fp64"))
+    (gottc, _), n = oz_launches(lambda: eff_ham_mul_state(effg, th, "cent", "fp64tc"))
+    assert n > 0, "the tensor-core kernel did not run"
+    e64, etc = rel_err(got64, ref), rel_err(gottc, ref)
+    print(f"fp64 {e64:.2e} fp64tc {etc:.2e}")
+    assert e64 <= 1e-13
+    assert etc <= TOL, (e64, etc)
+
+
 def test_fp64tc_lanczos_energy_matches_fp64_same_problem(lib):
     """The reference's Lanczos set-up (``test_lanczos_solver.cc:121-153``:
     symmetric environments, one sector per leg) at D=256, 7 Lanczos steps

@@ -222,15 +222,22 @@ def _scale_leg(t, leg, s):
 
 @pytest.mark.parametrize("scale_side", [1, 2])
 @pytest.mark.parametrize("big_side", ["l", "r"])
-def test_svd_gram_routes_match_oracle(lib, scale_side, big_side):
+@pytest.mark.parametrize("size", ["mid", "large"])
+def test_svd_gram_routes_match_oracle(lib, scale_side, big_side, size):
     """Groups of a few hundred rows on one side: the sweep's Gram routes
     ('r': U orthonormal, S.Vt returned; 'l': V orthonormal, U.S returned),
     on the canonical side's Gram matrix or -- when the other side is much
-    smaller -- on the other side's, against the oracle's SVD."""
+    smaller -- on the other side's, against the oracle's SVD.  The large
+    case (groups up to 1350 x 580) takes the Gram matrices and projections
+    through the FP64-accurate tensor-core contraction."""
     from mps2_gb300.vmps import SVD
     rng = np.random.default_rng(17 + scale_side)
-    big = Index([((-1,), 300), ((1,), 280)], IN)
-    small = Index([((-1,), 60), ((1,), 70)], IN)
+    if size == "mid":
+        big = Index([((-1,), 300), ((1,), 280)], IN)
+        small = Index([((-1,), 60), ((1,), 70)], IN)
+    else:
+        big = Index([((-1,), 700), ((1,), 650)], IN)
+        small = Index([((-1,), 300), ((1,), 280)], IN)
     l = big if big_side == "l" else small
     r = (small if big_side == "l" else big).inverse()
     s1 = Index([((1,), 1), ((-1,), 1)], OUT)
