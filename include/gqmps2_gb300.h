@@ -252,6 +252,13 @@ int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *para
 #define GQ_PROF_SVD 6     /* whole SVD, device span including library calls */
 #define GQ_PROF_SVD_EIG 7 /* its decompositions */
 int gq_profile_enable(int on);
+/* Tile-choice autotuner (not in the reference): with `on`, every matvec
+ * contraction whose block-size histogram has not been seen before times the
+ * candidate tensor-core thresholds on its real operands and keeps the
+ * fastest for all later contractions with that histogram (environment
+ * growth included).  Off by default: the fixed thresholds keep results
+ * bitwise reproducible from run to run. */
+int gq_autotune_enable(int on);
 int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes);
 /* The cudaStream_t all library work is queued on. */
 int gq_get_stream(void **stream);

@@ -83,6 +83,7 @@ EXPORTS = {
     "gq_dmrg_update": (_I, [_P, C.POINTER(SweepParamsC), _I, _I, C.POINTER(UpdateStatsC)]),
     "gq_dmrg_run_batch": (_I, [C.POINTER(_P), _I, C.POINTER(SweepParamsC), _I, _I, _DP]),
     "gq_tensor_dag": (_I, [_P, C.POINTER(_P)]),
+    "gq_autotune_enable": (_I, [_I]),
     "gq_mps_centralize": (_I, [C.POINTER(_P), _I, _I, _IP]),
     "gq_mps_truncate": (_I, [C.POINTER(_P), _I, _IP, C.c_double, C.c_int64, C.c_int64, _DP,
                              C.POINTER(C.c_int64)]),

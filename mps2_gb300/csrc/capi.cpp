@@ -482,6 +482,10 @@ int gq_dmrg_update(gq_dmrg *d, const gq_sweep_params *p, int dir, int target,
   });
 }
 
+int gq_autotune_enable(int on) {
+  return guarded([&] { gq::autotune_enable(on != 0); });
+}
+
 int gq_profile_enable(int on) {
   return guarded([&] {
     gq::ctx();

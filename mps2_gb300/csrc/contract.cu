@@ -13,7 +13,9 @@
 // bitwise-reproducible).  A block is used in place when its legs are already
 // ordered (free, contracted) or (contracted, free); otherwise one batched
 // permute kernel reorders all of its blocks first.
+#include <array>
 #include <map>
+#include <mutex>
 
 #include "gq_runtime.hpp"
 
@@ -96,7 +98,8 @@ void run_perm(const PermPlan &pp, const double *src, double *dst) {
 std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
                                             const std::vector<int> &axes_a,
                                             const std::vector<int> &axes_b,
-                                            const Tensor *target, Precision prec) {
+                                            const Tensor *target, Precision prec,
+                                            double tc_frac) {
   const int ra = a.rank(), rb = b.rank(), nc = (int)axes_a.size();
   GQ_CHECK(nc == (int)axes_b.size() && nc >= 1, "contraction needs matching, non-empty axes");
   GQ_CHECK(a.nq == b.nq, "operands use different charge counts");
@@ -280,7 +283,8 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
       // FP64-accurate form: 128 x 96 tiles, about 35 times the FP64 rate
       const int TM = prec == kTF32x3 ? 128 : oz_tile_m();
       const int TN = prec == kTF32x3 ? 128 : oz_tile_n();
-      const double frac = prec == kTF32x3 ? 0.02 : 0.03;
+      const double frac = tc_frac >= 0.0 ? tc_frac : (prec == kTF32x3 ? 0.02 : 0.03);
+      plan->tc_frac = frac;
       double useful = 0.0, padded = 0.0;
       for (auto &cp : kv.second) {
         int64_t k = 1;
@@ -295,6 +299,32 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
     any_tc |= tc;
     any_fp |= !tc;
     obs.push_back({ob, m, n, &kv.second, tc});
+  }
+  // autotuner key: the 16 heaviest output blocks' (log2 m, log2 n, log2 k of
+  // their largest pair) and log2 of the block count, hashed (FNV-1a)
+  {
+    std::vector<std::array<int, 4>> h;
+    for (auto &b0 : obs) {
+      int64_t kmax = 1;
+      for (auto &cp : *b0.pairs) {
+        int64_t k = 1;
+        for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
+        kmax = std::max(kmax, k);
+      }
+      auto lg = [](int64_t x) { int r = 0; while ((x >>= 1) > 0) ++r; return r; };
+      h.push_back({lg(b0.m) + lg(b0.n) + lg(kmax), lg(b0.m), lg(b0.n), lg(kmax)});
+    }
+    std::sort(h.begin(), h.end(), [](const std::array<int, 4> &x, const std::array<int, 4> &y) {
+      return x > y;
+    });
+    uint64_t hs = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { hs = (hs ^ v) * 1099511628211ull; };
+    int nb = 0;
+    for (int64_t x = (int64_t)obs.size(); x > 1; x >>= 1) ++nb;
+    mix((uint64_t)nb);
+    for (size_t i = 0; i < h.size() && i < 16; ++i)
+      for (int j = 1; j < 4; ++j) mix((uint64_t)h[i][j]);
+    plan->signature = hs;
   }
   // target blocks without contributions are written as zeros by FP64 tiles
   for (int64_t ob = 0; ob < o.nblocks(); ++ob)
@@ -549,9 +579,46 @@ void check_device_errors() {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner cache (process-wide; lanes share it)
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_tune_mu;
+std::map<std::pair<uint64_t, int>, double> g_tune;
+bool g_tune_on = false;
+}  // namespace
+
+// Tensor-core thresholds tried by the autotuner; the last one (above 1)
+// keeps every block on the FP64 kernel.
+const double kTuneCandidates[5] = {0.005, 0.02, 0.08, 0.3, 2.0};
+
+void autotune_enable(bool on) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_on = on;
+}
+bool autotune_on() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  return g_tune_on;
+}
+bool autotune_lookup(uint64_t sig, Precision prec, double *frac) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find({sig, (int)prec});
+  if (it == g_tune.end()) return false;
+  *frac = it->second;
+  return true;
+}
+void autotune_store(uint64_t sig, Precision prec, double frac) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[{sig, (int)prec}] = frac;
+}
+
 TensorPtr contract(const Tensor &a, const Tensor &b, const std::vector<int> &axes_a,
                    const std::vector<int> &axes_b, Precision prec, double *flops_out) {
   auto plan = plan_contract(a, b, axes_a, axes_b, nullptr, prec);
+  double frac;
+  if (prec != kFP64 && !plan->use_skinny && autotune_on() &&
+      autotune_lookup(plan->signature, prec, &frac) && frac != plan->tc_frac)
+    plan = plan_contract(a, b, axes_a, axes_b, nullptr, prec, frac);
   auto out = clone_structure(*plan->out);
   out->allocate();
   DevBuf scratch(contract_scratch(*plan));

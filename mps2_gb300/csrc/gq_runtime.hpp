@@ -176,15 +176,33 @@ struct ContractPlan {
   double flops = 0.0;         // 2*m*n*k summed over block products
   int64_t a_elems = 0, b_elems = 0;
   int tile_m = 0, tile_n = 0;
+  uint64_t signature = 0;     // block-size histogram hash (autotuner key)
+  double tc_frac = 0.0;       // threshold the plan was built with
 };
 
 // Plan C = A . B over the given axes.  If `target` is non-null the output
 // uses its structure (every contributing block must exist there; blocks of
 // `target` without contributions are written as zeros).
+// `tc_frac` < 0: the default share of useful work at which an output block
+// goes to the tensor-core kernel (2% for 3xTF32, 3% for FP64TC); otherwise
+// that share (an autotuned value).
 std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
                                             const std::vector<int> &axes_a,
                                             const std::vector<int> &axes_b,
-                                            const Tensor *target, Precision prec);
+                                            const Tensor *target, Precision prec,
+                                            double tc_frac = -1.0);
+
+// Tile-choice autotuner.  A contraction's signature is a hash of its
+// block-size histogram (the output blocks' log2 m, n, k, heaviest first);
+// for a new signature the candidate tensor-core thresholds are timed on the
+// real operands once and the fastest is kept for every later contraction
+// with that signature.  Off by default (the choice then follows fixed
+// thresholds and results are bitwise reproducible run to run).
+void autotune_enable(bool on);
+bool autotune_on();
+bool autotune_lookup(uint64_t signature, Precision prec, double *tc_frac);
+void autotune_store(uint64_t signature, Precision prec, double tc_frac);
+extern const double kTuneCandidates[5];
 // Scratch needed by run_contract (elements).
 int64_t contract_scratch(const ContractPlan &p);
 void run_contract(const ContractPlan &p, const double *a, const double *b, double *c,

@@ -7,6 +7,7 @@
 // matvec follows ``eff_ham_mul_state_{cent,lend,rend}`` (``:228-256``)
 // contraction for contraction; its work lists are planned once per update
 // and replayed every iteration.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -90,6 +91,52 @@ int64_t eff_ham_dim(const EffHam &h) {
   }
 }
 
+namespace {
+// Autotuning of one matvec step: every candidate threshold that gives a
+// different kernel split is timed (one warm-up run, one timed run, CUDA
+// events) on the step's real operands; the fastest is stored under the
+// plan's signature and returned.
+std::shared_ptr<ContractPlan> tune_step(const Tensor &A, const double *a, bool a_const,
+                                        const Tensor &B, const double *b, bool b_const,
+                                        const std::vector<int> &xa, const std::vector<int> &xb,
+                                        const Tensor *target, Precision prec,
+                                        std::shared_ptr<ContractPlan> first) {
+  auto s = stream();
+  cudaEvent_t e0, e1;
+  GQ_CUDA(cudaEventCreate(&e0));
+  GQ_CUDA(cudaEventCreate(&e1));
+  std::shared_ptr<ContractPlan> best;
+  float best_ms = 0.f;
+  std::vector<std::pair<int64_t, int64_t>> seen;
+  DevBuf out(first->out->size());
+  for (double frac : kTuneCandidates) {
+    auto pl = plan_contract(A, B, xa, xb, target, prec, frac);
+    const std::pair<int64_t, int64_t> split{pl->ntiles_tc + pl->ntiles_oz, pl->ntiles};
+    if (std::find(seen.begin(), seen.end(), split) != seen.end()) continue;
+    seen.push_back(split);
+    if (a_const) cache_operand(*pl, 0, a);
+    if (b_const) cache_operand(*pl, 1, b);
+    DevBuf scratch(contract_scratch(*pl));
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {
+      GQ_CUDA(cudaEventRecord(e0, s));
+      run_contract(*pl, a, b, out.p, scratch.p, prec);
+      GQ_CUDA(cudaEventRecord(e1, s));
+      GQ_CUDA(cudaEventSynchronize(e1));
+      GQ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    if (!best || ms < best_ms) {
+      best = pl;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  autotune_store(first->signature, prec, best->tc_frac);
+  return best;
+}
+}  // namespace
+
 std::shared_ptr<MatvecPlan> plan_matvec(const EffHam &h, const Tensor &space, Precision prec) {
   auto mp = std::make_shared<MatvecPlan>();
   mp->h = h;
@@ -118,10 +165,22 @@ std::shared_ptr<MatvecPlan> plan_matvec(const EffHam &h, const Tensor &space, Pr
     const Tensor &B = s.bs == -2 ? *s.cb : (s.bs == -1 ? space : *mp->inter[s.bs]);
     const bool last = i + 1 == spec.size();
     auto plan = plan_contract(A, B, s.xa, s.xb, last ? &space : nullptr, prec);
+    const double *a_data = A.data.p, *b_data = B.data.p;
+    const bool tuned = prec != kFP64 && !plan->use_skinny && autotune_on();
+    if (tuned) {
+      double frac;
+      if (autotune_lookup(plan->signature, prec, &frac)) {
+        if (frac != plan->tc_frac)
+          plan = plan_contract(A, B, s.xa, s.xb, last ? &space : nullptr, prec, frac);
+      } else {
+        plan = tune_step(A, a_data, s.as == -2, B, b_data, s.bs == -2, s.xa, s.xb,
+                         last ? &space : nullptr, prec, plan);
+      }
+    }
     // Environments and MPO tensors do not change during the solve: pack
     // them for the tensor cores once.
-    if (s.as == -2) cache_operand(*plan, 0, s.ca->data.p);
-    if (s.bs == -2) cache_operand(*plan, 1, s.cb->data.p);
+    if (s.as == -2 && !plan->a_cached && !plan->a_oz_cached) cache_operand(*plan, 0, a_data);
+    if (s.bs == -2 && !plan->b_cached && !plan->b_oz_cached) cache_operand(*plan, 1, b_data);
     MatvecStep st;
     st.plan = plan;
     st.a_src = s.as;
@@ -135,6 +194,11 @@ std::shared_ptr<MatvecPlan> plan_matvec(const EffHam &h, const Tensor &space, Pr
       t->allocate();
       mp->inter.push_back(t);
       st.out = (int)mp->inter.size() - 1;
+      if (autotune_on() && prec != kFP64) {
+        // the next step is tuned on real data: run this one now
+        DevBuf scratch(contract_scratch(*plan));
+        run_contract(*plan, a_data, b_data, t->data.p, scratch.p, prec);
+      }
     }
     scratch = std::max(scratch, contract_scratch(*plan));
     mp->flops += plan->flops;

@@ -191,6 +191,12 @@ def TwoSiteFiniteVMPS(mps: FiniteMPS, mpo: Sequence[GQTensor], sweep_params: Swe
     return e0
 
 
+def autotune_enable(on: bool = True) -> None:
+    """Tile-choice autotuner keyed on each contraction's block-size histogram
+    (``gq_autotune_enable``); off by default."""
+    check(load().gq_autotune_enable(1 if on else 0))
+
+
 def profile_enable(on: bool = True) -> None:
     check(load().gq_profile_enable(1 if on else 0))
 
