@@ -27,6 +27,12 @@ with a seed-0 shuffled site order; the bond dimension grows
   update (block structure recorded from a GPU run), the reference's own
   gqten+MKL path being unbuildable here.
 
+Other workloads (not the headline line): ``--model hubbard`` (L=64 Fermi-
+Hubbard chain, t=1, U=8, half filling, D 1000 -> 4000 over 8 sweeps) and
+``--workload batched`` (64 seeded XXZ chains, L in [16, 64], Delta in
+[0.5, 1.5], D in {64..512}, 4 sweeps each, run concurrently and one after
+another; the metric is instances per second).
+
 Multi-GPU: a sweep is a sequential chain of updates, so N>1 runs N
 independent replicas (one per rank); value is the max over ranks.
 """
