@@ -42,11 +42,14 @@ struct MatvecPlan {
 };
 
 namespace {
-// Graph replay of the matvec, unless the kernel profiler is on (it times
-// every launch with its own events) or GQ_NO_GRAPHS is set.
+// Graph replay of the matvec on the main lane, unless the kernel profiler
+// is on (it times every launch with its own events) or GQ_NO_GRAPHS is set.
+// Not on the lanes of a batched run: there every solve's capture and
+// instantiation contend across the host threads (64 XXZ chains: 26.2 s with
+// graphs, 19.3 s without; one chain after another: 107 s vs 109 s).
 bool graphs_enabled() {
   static const bool off = std::getenv("GQ_NO_GRAPHS") != nullptr;
-  return !off && !prof_on();
+  return !off && !prof_on() && on_main_lane();
 }
 
 void run_matvec_graph(MatvecPlan &p, const double *x, double *y, double *xin, int64_t n) {
