@@ -50,7 +50,9 @@ enum ProfKernel : int {
   kProfGemmFp64Tc = 5, // FP64-accurate exact-slice tcgen05 grouped GEMM
   kProfSvd = 6,        // whole truncating SVD (device span, library calls included)
   kProfSvdEig = 7,     // its decompositions (cuSOLVER eigensolves / Jacobi, Gram GEMMs)
-  kProfCount = 8,
+  kProfSvdGather = 8,  // its gather of the groups into dense matrices
+  kProfSvdFactors = 9, // its factor assembly (copies, projections, sign fix, completion)
+  kProfCount = 10,
 };
 bool prof_on();
 void prof_enable(bool on);

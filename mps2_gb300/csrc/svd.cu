@@ -459,6 +459,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   GQ_CHECK(!groups.empty(), "SVD of a tensor without blocks");
 
   // ---- gather each group into a dense row-major m x n matrix --------------
+  prof_begin(kProfSvdGather);
   DevBuf mats(mat_total);
   GQ_CUDA(cudaMemsetAsync(mats.p, 0, sizeof(double) * mat_total, s));
   {
@@ -472,6 +473,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     }
     launch_items(gather_kernel, items, t.data.p, mats.p);
   }
+  prof_end(kProfSvdGather, 0.0, 0.0);
 
   // ---- decompositions -----------------------------------------------------
   prof_begin(kProfSvdEig);
@@ -746,6 +748,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   GQ_CHECK(!sectors.empty(), "SVD kept no singular value");
 
   // ---- factors L (m x keep) and R (n x keep) per group ------------------------
+  prof_begin(kProfSvdFactors);
   // 'r' (scale_side 2): L = U, R = (S.Vt)^T; 'l' (1): L = U.S, R = V;
   // plain (0): L = U, R = V.  Columns of kept zero values start at zero.
   DevBuf Lb(L_total), Rb(R_total);
@@ -871,6 +874,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     if (scale_side != 2) completion(false, Rb.p + g->R_off + g->keep_nz * g->n);
   }
 
+  prof_end(kProfSvdFactors, 0.0, 0.0);
   // ---- output tensors ---------------------------------------------------------
   Index nb;
   nb.dir = 1;
