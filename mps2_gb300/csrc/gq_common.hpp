@@ -108,6 +108,9 @@ struct Index {
 // Device memory: stream-ordered allocations from CUDA's pool allocator.
 // ---------------------------------------------------------------------------
 cudaStream_t stream();  // the library's compute stream
+// Stream-ordered host-to-device copy of a host buffer the caller may reuse
+// as soon as this returns (staged through pinned memory; runtime.cu).
+void upload_async(void *dst, const void *src, size_t bytes);
 
 struct DevBuf {
   double *p = nullptr;
@@ -144,7 +147,7 @@ struct DevArray {  // small typed device arrays for work lists
     n = (int64_t)h.size();
     if (n == 0) return;
     GQ_CUDA(cudaMallocAsync((void **)&p, sizeof(T) * n, stream()));
-    GQ_CUDA(cudaMemcpyAsync(p, h.data(), sizeof(T) * n, cudaMemcpyHostToDevice, stream()));
+    upload_async(p, h.data(), sizeof(T) * n);
   }
   void release() {
     if (p) cudaFreeAsync(p, stream());

@@ -21,6 +21,8 @@ struct Lane {
   double *dev_scalars = nullptr;   // device, 64 doubles; [63] = tensor-core error word
   void *cusolver = nullptr;        // cusolverDnHandle_t, created lazily
   void *cublas = nullptr;          // cublasHandle_t, created lazily
+  char *staging = nullptr;         // pinned ring for work-list uploads
+  size_t staging_head = 0;
 };
 
 struct Context {

@@ -2,6 +2,7 @@
 #include "gq_runtime.hpp"
 
 #include <cstdio>
+#include <cstring>
 #include <map>
 #include <mutex>
 
@@ -74,6 +75,7 @@ void lane_destroy(Lane *l) {
   cudaFreeAsync(l->dev_scalars, l->stream);
   cudaStreamSynchronize(l->stream);
   cudaFreeHost(l->host_scalars);
+  if (l->staging) cudaFreeHost(l->staging);
   cudaStreamDestroy(l->stream);
   delete l;
 }
@@ -83,6 +85,37 @@ void lane_bind(Lane *l) { t_lane = l; }
 bool on_main_lane() { return t_lane == nullptr; }
 
 cudaStream_t stream() { return lane().stream; }
+
+// Work lists (tiles, pairs, pack tasks...) go to the device while kernels
+// run.  A cudaMemcpyAsync from pageable memory synchronises the stream
+// first, which would drain the GPU at every plan built between two kernels
+// (the SVD's projections and the environment growth build several); the
+// lists are staged through a pinned ring per lane instead.  Regions of the
+// ring are reused only after it wraps, behind a stream synchronisation.
+namespace {
+constexpr size_t kStagingBytes = size_t(16) << 20;
+}
+
+void upload_async(void *dst, const void *src, size_t bytes) {
+  Lane &l = lane();
+  if (bytes == 0) return;
+  if (bytes > kStagingBytes) {  // rare: plain (synchronising) copy
+    GQ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, l.stream));
+    return;
+  }
+  if (!l.staging) {
+    GQ_CUDA(cudaMallocHost((void **)&l.staging, kStagingBytes));
+    l.staging_head = 0;
+  }
+  size_t off = (l.staging_head + 255) & ~size_t(255);
+  if (off + bytes > kStagingBytes) {
+    GQ_CUDA(cudaStreamSynchronize(l.stream));
+    off = 0;
+  }
+  std::memcpy(l.staging + off, src, bytes);
+  GQ_CUDA(cudaMemcpyAsync(dst, l.staging + off, bytes, cudaMemcpyHostToDevice, l.stream));
+  l.staging_head = off + bytes;
+}
 
 void sync() { GQ_CUDA(cudaStreamSynchronize(stream())); }
 
