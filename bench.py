@@ -374,7 +374,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     prof_sweep_s = ev0.elapsed_time(ev1) * 1e-3
     prof = {k: profile_read(k) for k in FAMILIES}
-    svd_span = {k: profile_read(k) for k in ("svd", "svd_eig", "svd_gather", "svd_factors")}
+    svd_span = {k: profile_read(k) for k in ("svd", "svd_eig", "svd_gather", "svd_factors",
+                                              "svd_ortho")}
     profile_enable(False)
     n_launch_ours = sum(v[0] for v in prof.values())
 
@@ -485,7 +486,9 @@ def run_ours(args):
                          "svd_device_span": svd_span["svd"][1] * 1e-3,
                          "svd_decompositions": svd_span["svd_eig"][1] * 1e-3,
                          "svd_gather": svd_span["svd_gather"][1] * 1e-3,
-                         "svd_factors": svd_span["svd_factors"][1] * 1e-3},
+                         "svd_factors": svd_span["svd_factors"][1] * 1e-3,
+                         "svd_ortho": svd_span["svd_ortho"][1] * 1e-3,
+                         "svd_ortho_calls": svd_span["svd_ortho"][0]},
         "central_problem": {"fp64": solve["fp64"], "tf32x3": solve["tf32x3"],
                             "fp64tc": solve["fp64tc"],
                             "delta_e_rel": de,

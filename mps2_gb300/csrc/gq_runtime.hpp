@@ -54,7 +54,8 @@ enum ProfKernel : int {
   kProfSvdEig = 7,     // its decompositions (cuSOLVER eigensolves / Jacobi, Gram GEMMs)
   kProfSvdGather = 8,  // its gather of the groups into dense matrices
   kProfSvdFactors = 9, // its factor assembly (copies, projections, sign fix, completion)
-  kProfCount = 10,
+  kProfSvdOrtho = 10,  // of which: CholeskyQR2 of transposed-route factors
+  kProfCount = 11,
 };
 bool prof_on();
 void prof_enable(bool on);

@@ -258,36 +258,6 @@ void normalise_columns(double *q, int64_t dim, int64_t k) {
   GQ_CUDA(cudaGetLastError());
 }
 
-// CholeskyQR2: the k columns of q (dim x k, ld dim) replaced by an
-// orthonormal basis of their span (q <- q R^-1 twice, R from the Cholesky
-// factor of q^T q).
-void cholqr2(double *q, int64_t dim, int64_t k) {
-  if (k == 0) return;
-  auto s = stream();
-  auto bh = blas();
-  auto sh = solver();
-  const int d = (int)dim, kk = (int)k;
-  const double one = 1.0, zero = 0.0;
-  DevBuf g(k * k);
-  int lw = 0;
-  GQ_SOLVER(cusolverDnDpotrf_bufferSize(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, &lw));
-  DevBuf work((int64_t)lw + 1);
-  DevArray<int> info;
-  info.upload(std::vector<int>(2, 0));
-  for (int pass = 0; pass < 2; ++pass) {
-    GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, kk, kk, d, &one, q, d, q, d, &zero, g.p,
-                        kk));
-    GQ_SOLVER(cusolverDnDpotrf(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, work.p, lw,
-                               info.p + pass));
-    GQ_BLAS(cublasDtrsm(bh, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                        CUBLAS_DIAG_NON_UNIT, d, kk, &one, g.p, kk, q, d));
-  }
-  int hinfo[2] = {0, 0};
-  GQ_CUDA(cudaMemcpyAsync(hinfo, info.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
-  sync();
-  if (hinfo[0] != 0 || hinfo[1] != 0) fail(kSolverError, "CholeskyQR2: Cholesky failed");
-}
-
 // Dense FP64 products of the large groups on the FP64-accurate tensor-core
 // path: A (a0 x a1) and B (b0 x b1) row-major, contracted over A's axis
 // `axa` and B's axis `axb`; C (the two free dimensions, A's first) written
@@ -320,6 +290,40 @@ void dense_contract_tc(const double *A, int64_t a0, int64_t a1, int axa, const d
   auto tc = contract(*ta, *tb, {axa}, {axb}, kFP64TC);
   GQ_CUDA(cudaMemcpyAsync(C, tc->data.p, sizeof(double) * tc->size(), cudaMemcpyDeviceToDevice,
                           stream()));
+}
+
+// CholeskyQR2: the k columns of q (dim x k, ld dim) replaced by an
+// orthonormal basis of their span (q <- q R^-1 twice, R from the Cholesky
+// factor of q^T q).
+void cholqr2(double *q, int64_t dim, int64_t k) {
+  if (k == 0) return;
+  auto s = stream();
+  auto bh = blas();
+  auto sh = solver();
+  const int d = (int)dim, kk = (int)k;
+  const double one = 1.0, zero = 0.0;
+  DevBuf g(k * k);
+  int lw = 0;
+  GQ_SOLVER(cusolverDnDpotrf_bufferSize(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, &lw));
+  DevBuf work((int64_t)lw + 1);
+  DevArray<int> info;
+  info.upload(std::vector<int>(2, 0));
+  const bool tc = 2.0 * (double)k * (double)k * (double)dim >= kTcMinFlops;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (tc)  // q col-major d x k = row-major k x d: G = q^T q = Qrow Qrow^T
+      dense_contract_tc(q, k, dim, 1, q, k, dim, 1, g.p);
+    else
+      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, kk, kk, d, &one, q, d, q, d, &zero, g.p,
+                          kk));
+    GQ_SOLVER(cusolverDnDpotrf(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, work.p, lw,
+                               info.p + pass));
+    GQ_BLAS(cublasDtrsm(bh, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                        CUBLAS_DIAG_NON_UNIT, d, kk, &one, g.p, kk, q, d));
+  }
+  int hinfo[2] = {0, 0};
+  GQ_CUDA(cudaMemcpyAsync(hinfo, info.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  sync();
+  if (hinfo[0] != 0 || hinfo[1] != 0) fail(kSolverError, "CholeskyQR2: Cholesky failed");
 }
 
 // Transposed Gram route for a group whose canonical side has `canon` rows
@@ -816,15 +820,19 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       if (g->route == kGramLeft) {
         if (!g->eig_m) {
           left_from_right();
+          prof_begin(kProfSvdOrtho);
           normalise_columns(L, m, k);
           cholqr2(L, m, k);
+          prof_end(kProfSvdOrtho, 0.0, 0.0);
         }
         right_from_left();
       } else {
         if (g->eig_m) {
           right_from_left();
+          prof_begin(kProfSvdOrtho);
           normalise_columns(R, n, k);
           cholqr2(R, n, k);
+          prof_end(kProfSvdOrtho, 0.0, 0.0);
         }
         left_from_right();
       }
