@@ -445,12 +445,21 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
           for (int j = 0; j < 32; ++j) v[j] += (double)__uint_as_float(f[j]);
         }
         if (row < t.m) {
+          // all 32 loads of the running sums first (independent, in flight
+          // together), then the adds and stores
+          const int cbase = t.col0 + cb * 32;
+          if (c > 0) {
+            double old[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) old[j] = (cbase + j < t.n) ? crow[cbase + j] : 0.0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] += old[j];
+          }
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const int cl = cb * 32 + j, col = t.col0 + cl;
+            const int cl = cb * 32 + j, col = cbase + j;
             if (col < t.n) {
               double x = v[j];
-              if (c > 0) x += crow[col];
               if (last) {
                 const int ec = sm.colexp[cl];
                 x = (oz::valid_exp(er) && oz::valid_exp(ec)) ? ldexp(x, er + ec - 14) : 0.0;
