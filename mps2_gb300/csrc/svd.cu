@@ -16,7 +16,9 @@
 //  * kept nonzero values: the largest-|.| entry of each left vector is made
 //    positive (the right vector follows); kept zero values use the
 //    canonical completion of null_completion (a counter-hashed seed matrix
-//    projected off the group's nonzero singular vectors, then CholeskyQR2);
+//    projected off the group's nonzero singular vectors, then CholeskyQR2)
+//    -- except on a Gram route that solved the canonical side, where the
+//    eigenvectors of the zero eigenvalues serve (see below);
 //  * new bond sectors: groups with a kept value, ascending charge.
 //
 // Decomposition routes (all FP64):
@@ -760,8 +762,16 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   GQ_CUDA(cudaMemsetAsync(Rb.p, 0, sizeof(double) * R_total, s));
   const bool scale_l = scale_side == 1, scale_r = scale_side == 2;
   std::vector<ColItem> l_small, r_small, l_jac, r_jac, l_ev, r_ev;
+  // A Gram route whose eigensolve ran on the canonical side supplies that
+  // side's columns for kept zero values too: the eigenvectors of the
+  // zero (below-floor) eigenvalues are orthonormal and orthogonal to the
+  // kept nonzero ones, which is all the completion has to provide.
+  auto eig_is_canonical = [](const Group *g) {
+    return (g->route == kGramLeft && g->eig_m) || (g->route == kGramRight && !g->eig_m);
+  };
   for (Group *g : groups) {
-    for (int64_t j = 0; j < g->keep_nz; ++j) {
+    const int64_t ncopy = eig_is_canonical(g) ? g->keep : g->keep_nz;
+    for (int64_t j = 0; j < ncopy; ++j) {
       const int sc = g->src_cols[j];
       const double sj = g->svals[j];
       switch (g->route) {
@@ -878,6 +888,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       launch_items(col_copy_kernel, items, src, q.p);
       null_completion(q.p, dim, g->nnz, kz, (int)gi, left ? 0 : 1, dst);
     };
+    if (eig_is_canonical(g)) continue;  // zero columns came with the eigenvectors
     if (scale_side != 1) completion(true, Lb.p + g->L_off + g->keep_nz * g->m);
     if (scale_side != 2) completion(false, Rb.p + g->R_off + g->keep_nz * g->n);
   }
