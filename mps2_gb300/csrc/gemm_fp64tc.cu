@@ -588,13 +588,11 @@ void run_oz_pack(const OzPackPlan &pp, const double *src, const OzPacked &dst) {
 
 void launch_gemm_fp64tc(const ContractPlan &p, const OzPacked &A, const OzPacked &B, double *C) {
   if (p.ntiles_oz == 0) return;
-  static bool attr = false;
   const size_t smem = sizeof(OzSmem) + 1024;
-  if (!attr) {
-    GQ_CUDA(cudaFuncSetAttribute(gemm_fp64tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
+  // once per process, whichever lane launches first
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      gemm_fp64tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  GQ_CUDA(attr);
   prof_begin(kProfGemmFp64Tc);
   gemm_fp64tc_kernel<<<(unsigned)p.ntiles_oz, oz::kThreads, smem, stream()>>>(
       p.tiles_oz.p, p.pairs_oz.p, A.data, B.data, A.rowexp, B.rowexp, C, tc_error_flag());

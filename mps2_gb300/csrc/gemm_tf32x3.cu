@@ -512,13 +512,11 @@ void run_tc_pack(const TcPackPlan &pp, const double *src, float *dst) {
 }
 
 void launch_gemm_tf32x3(const ContractPlan &p, const float *A, const float *B, double *C) {
-  static bool attr = false;
   const size_t smem = sizeof(TcSmem) + 1024;
-  if (!attr) {
-    GQ_CUDA(cudaFuncSetAttribute(gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
+  // once per process, whichever lane launches first
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  GQ_CUDA(attr);
   int *err = tc_error_flag();
   prof_begin(kProfGemmTf32);
   gemm_tf32x3_kernel<<<(unsigned)p.ntiles_tc, tc::kThreads, smem, stream()>>>(

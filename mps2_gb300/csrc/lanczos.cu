@@ -105,9 +105,16 @@ std::shared_ptr<ContractPlan> tune_step(const Tensor &A, const double *a, bool a
                                         const Tensor *target, Precision prec,
                                         std::shared_ptr<ContractPlan> first) {
   auto s = stream();
-  cudaEvent_t e0, e1;
-  GQ_CUDA(cudaEventCreate(&e0));
-  GQ_CUDA(cudaEventCreate(&e1));
+  struct Events {  // released on every exit path
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Events() {
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+  } ev;
+  GQ_CUDA(cudaEventCreate(&ev.e0));
+  GQ_CUDA(cudaEventCreate(&ev.e1));
+  cudaEvent_t e0 = ev.e0, e1 = ev.e1;
   std::shared_ptr<ContractPlan> best;
   float best_ms = 0.f;
   std::vector<std::pair<int64_t, int64_t>> seen;
@@ -133,8 +140,6 @@ std::shared_ptr<ContractPlan> tune_step(const Tensor &A, const double *a, bool a
       best_ms = ms;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   autotune_store(first->signature, prec, best->tc_frac);
   return best;
 }
