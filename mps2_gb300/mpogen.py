@@ -4,58 +4,49 @@ API mirrors ``include/gqmps2/one_dim_tn/mpo/mpogen/mpogen.h:40-121``:
 ``AddTerm`` in its three overloads (generic operator string at
 ``mpogen_impl.h:86-121``; physical operators with insertion operators such as
 a Jordan-Wigner string at ``:143-197``; one- or two-body shorthand at
-``:213-243``) and ``Gen`` (``:246-285``).
+``:213-243``), ``GetFSM`` and ``Gen`` (``:246-285``).
 
-Construction (this project's own): every term becomes a path through a
-finite-state automaton whose states live on the bonds.  Paths share a state
-while they have applied the same operators starting from the same head
-site (prefix sharing), so e.g. a nearest-neighbour Heisenberg chain gets the
-familiar 5 states per bond (ready, S^z, S^+, S^-, final) and a Hubbard chain
-with four hopping channels gets 6.  The term's coefficient is folded into
-the operator on its last site so that prefixes stay shareable; transitions
-into the final state add up.  The MPO matrices that come out have the
-reference's layout:
+The construction is the reference's, step for step, so the MPO tensors come
+out element for element as gqmps2 builds them:
 
-* bond states ordered [ready, intermediate states in creation order, final],
-  then grouped by quantum number in order of first appearance, one sector
-  per distinct QN (as ``SortSparOpReprMatColsByQN_``, ``mpogen_impl.h:300-349``);
-* the QN of the state reached through operator ``O`` from a state with QN
-  ``q`` is ``q - Div(O)`` (``CalcTgtRvbQN_``, ``:288-297``);
-* leg orders head ``(p_in, r, p_out)``, bulk ``(l, p_in, p_out, r)``, tail
-  ``(p_in, l, p_out)`` (``:359, :377, :398``), l IN and r OUT.
-
-The bond dimensions can differ from the reference's symbolic compression
-(``fsm.h:232-241`` plus ``symb_alg/coef_op_alg.h``) for long-range terms;
-the Hamiltonian represented is the same.
+* every term becomes a path of the finite-state machine (``fsm.FSM``), with
+  the term's coefficient label on its first operator (``:97-115``);
+  coefficients and operators are labelled in order of first appearance,
+  coefficient 1 and the first site's identity taking label 0
+  (``:64-72``); two operators are the same when their legs and elements are
+  equal;
+* the machine's symbolic matrices are compressed (``FSM::GenCompressedMatRepr``,
+  columns left to right, rows right to left);
+* the columns of each site's matrix are grouped by the quantum number of the
+  bond state, groups in order of first appearance, and within a group the
+  later column first (``SortSparOpReprMatColsByQN_``, ``:300-349``); the QN
+  of a column reached through operator ``O`` from a row with QN ``q`` is
+  ``q - Div(O)`` (``CalcTgtRvbQN_``, ``:288-297``); the next site's rows
+  follow the same permutation (``:269, :275``);
+* each symbolic element is realised as ``sum_i c_i * O_i`` and written into
+  the MPO tensor where it is nonzero (``:352-451``): head ``(p_in, r, p_out)``,
+  bulk ``(l, p_in, p_out, r)``, tail ``(p_in, l, p_out)``, l IN and r OUT.
 """
 from __future__ import annotations
 
-from typing import Dict, List, Sequence
+from typing import List, Sequence
 
 import numpy as np
 
+from .fsm import FSM, LabelConvertor
 from .site_vec import SiteVec
+from .symb_alg import OpRepr, SparOpReprMat, kNullOpRepr
 from .tensor import GQTensor, Index, OUT, QN, Div
 
 
-class _OpTable:
-    """Interns dense operator matrices so equal operators share an id."""
+def _op_key(op: GQTensor):
+    """Equality of operators: same legs, same elements (0.0 == -0.0)."""
+    dense = op.to_dense() + 0.0
+    return (tuple(op.indices), dense.shape, dense.tobytes())
 
-    def __init__(self):
-        self.mats: List[np.ndarray] = []
-        self.divs: List[QN] = []
-        self._lut: Dict[tuple, int] = {}
 
-    def add(self, op: GQTensor) -> int:
-        dense = op.to_dense()
-        key = (dense.shape, dense.tobytes())
-        i = self._lut.get(key)
-        if i is None:
-            i = len(self.mats)
-            self._lut[key] = i
-            self.mats.append(dense)
-            self.divs.append(Div(op))
-        return i
+def _coef_key(c):
+    return float(c)
 
 
 class MPOGenerator:
@@ -65,10 +56,15 @@ class MPOGenerator:
         self.zero_div = QN(zero_div)
         self.pb_out = list(site_vec.sites)
         self.pb_in = [ix.inverse() for ix in self.pb_out]
-        self.ops = _OpTable()
-        self.id_ids = [self.ops.add(op) for op in site_vec.id_ops]
-        # (coef, head, [op id per site head..tail])
-        self.terms: List[tuple] = []
+        self.id_ops = list(site_vec.id_ops)
+        self.fsm_ = FSM(self.N)
+        self.op_label_convertor_ = LabelConvertor(self.id_ops[0], key=_op_key)
+        self.fsm_.ReplaceIdOpLabels([self.op_label_convertor_.Convert(o) for o in self.id_ops])
+        self.coef_label_convertor_ = LabelConvertor(1.0, key=_coef_key)
+        self.bond_dims: List[int] = []
+
+    def GetFSM(self) -> FSM:
+        return self.fsm_
 
     # ------------------------------------------------------------------
     def AddTerm(self, coef, *args, **kw):
@@ -131,127 +127,92 @@ class MPOGenerator:
         operator given for it is used, as the reference's ``std::find``
         lookup at ``:102`` does (this is what happens to the tail string's
         entry on the last physical site)."""
-        if coef == 0:
-            return
         if len(ops) != len(idxs) or not ops:
             raise ValueError("operators and site indexes differ in length")
         if list(idxs) != sorted(idxs):
             raise ValueError("site indexes must be ascending")
         if idxs[-1] >= self.N:
             raise ValueError("site index out of range")
+        if coef == 0:
+            return
+        coef_label = self.coef_label_convertor_.Convert(coef)
         head, tail = idxs[0], idxs[-1]
-        per_site: Dict[int, GQTensor] = {}
-        for op, s in zip(ops, idxs):
-            if s not in per_site:
-                per_site[s] = op
-        chain = []
+        reprs = []
         for s in range(head, tail + 1):
-            chain.append(self.ops.add(per_site[s]) if s in per_site else self.id_ids[s])
-        self.terms.append((float(coef), head, chain))
+            if s in idxs:
+                loc = idxs.index(s)
+                label = self.op_label_convertor_.Convert(ops[loc])
+                reprs.append(OpRepr(coef_label, label) if loc == 0 else OpRepr(label))
+            else:
+                reprs.append(OpRepr(self.op_label_convertor_.Convert(self.id_ops[s])))
+        self.fsm_.AddPath(head, tail, reprs)
 
     # ------------------------------------------------------------------
+    def _sort_cols_by_qn(self, m: SparOpReprMat, lvb: Index, ops: Sequence[GQTensor]):
+        """``SortSparOpReprMatColsByQN_``: permutes m's columns in place and
+        returns (permutation, right bond index)."""
+        groups: List[list] = []          # [qn, count]
+        order: List[int] = []
+        for y in range(m.cols):
+            col_qn = None
+            for x, elem in m.col_items(y):
+                q = self.zero_div - Div(ops[elem.ops[0]]) + lvb.qn_of_coor(x)
+                if col_qn is None:
+                    col_qn = q
+                    offset = 0
+                    for g in groups:
+                        if g[0] == q:
+                            g[1] += 1
+                            break
+                        offset += g[1]
+                    else:
+                        groups.append([q, 1])
+                    order.insert(offset, y)
+                elif q != col_qn:
+                    raise ValueError("operator breaks the quantum-number conservation "
+                                     f"(bond state {y} reached with two quantum numbers)")
+            if col_qn is None:
+                raise ValueError(f"bond state {y} has no incoming operator")
+        m.TransposeCols(order)
+        return order, Index([(q, n) for q, n in groups], OUT)
+
     def Gen(self) -> List[GQTensor]:
         N = self.N
         if N < 2:
             raise ValueError("an MPO needs at least two sites")
-        # states per bond b = 0..N-2 (bond b sits between site b and b+1)
-        mids: List[Dict[tuple, int]] = [dict() for _ in range(N - 1)]
-        mid_qn: List[List[QN]] = [[] for _ in range(N - 1)]
-        has_ready = [False] * (N - 1)
-        has_final = [False] * (N - 1)
+        mats = self.fsm_.GenCompressedMatRepr()
+        coefs = self.coef_label_convertor_.GetLabelObjMapping()
+        ops = self.op_label_convertor_.GetLabelObjMapping()
+        dense_ops = [o.to_dense() for o in ops]
+        self.bond_dims = [m.cols for m in mats[:-1]]
         zero = self.zero_div
-        # transitions[site] : dict (row_key, col_key) -> (op_id or dense, accumulate?)
-        trans: List[Dict[tuple, np.ndarray]] = [dict() for _ in range(N)]
-        set_once: List[Dict[tuple, int]] = [dict() for _ in range(N)]
-
-        def mid_key(head, chain, b):
-            return ("m", head, tuple(chain[: b - head + 1]))
-
-        for coef, head, chain in self.terms:
-            tail = head + len(chain) - 1
-            for b in range(0, head):
-                has_ready[b] = True
-            for b in range(tail, N - 1):
-                has_final[b] = True
-            q = zero
-            for s in range(head, tail + 1):
-                op_id = chain[s - head]
-                q = q - self.ops.divs[op_id]
-                row = ("ready",) if s == head else mid_key(head, chain, s - 1)
-                if s == tail:
-                    if q != zero:
-                        raise ValueError("term does not conserve the quantum number")
-                    key = (row, ("final",))
-                    mat = coef * self.ops.mats[op_id]
-                    if key in trans[s]:
-                        trans[s][key] = trans[s][key] + mat
-                    else:
-                        trans[s][key] = mat
-                else:
-                    col = mid_key(head, chain, s)
-                    if col not in mids[s]:
-                        mids[s][col] = len(mids[s])
-                        mid_qn[s].append(q)
-                    elif mid_qn[s][mids[s][col]] != q:
-                        raise ValueError("inconsistent intermediate quantum number")
-                    set_once[s][(row, col)] = op_id
-
-        # bond state lists: [ready, mids..., final], then grouped by QN
-        bond_states: List[List[tuple]] = []
-        bond_index: List[Index] = []
-        for b in range(N - 1):
-            states = []
-            if has_ready[b]:
-                states.append((("ready",), zero))
-            for key, pos in sorted(mids[b].items(), key=lambda kv: kv[1]):
-                states.append((key, mid_qn[b][pos]))
-            if has_final[b]:
-                states.append((("final",), zero))
-            order_qn: List[QN] = []
-            groups: Dict[QN, list] = {}
-            for key, q in states:
-                if q not in groups:
-                    groups[q] = []
-                    order_qn.append(q)
-                groups[q].append(key)
-            ordered = [k for q in order_qn for k in groups[q]]
-            bond_states.append(ordered)
-            bond_index.append(Index([(q, len(groups[q])) for q in order_qn], OUT))
-
-        # ready->ready and final->final identities
-        for s in range(N):
-            lrows = [("ready",)] if s == 0 else bond_states[s - 1]
-            rcols = [("final",)] if s == N - 1 else bond_states[s]
-            idm = self.ops.mats[self.id_ids[s]]
-            if ("ready",) in lrows and ("ready",) in rcols:
-                set_once[s][(("ready",), ("ready",))] = self.id_ids[s]
-            if ("final",) in lrows and ("final",) in rcols:
-                key = (("final",), ("final",))
-                trans[s][key] = trans[s].get(key, 0) + idm
-
+        vb = Index([(zero, 1)], OUT)
+        order: List[int] = []
         mpo: List[GQTensor] = []
         for s in range(N):
-            lrows = [("ready",)] if s == 0 else bond_states[s - 1]
-            rcols = [("final",)] if s == N - 1 else bond_states[s]
-            rpos = {k: i for i, k in enumerate(lrows)}
-            cpos = {k: i for i, k in enumerate(rcols)}
-            d = self.pb_out[s].dim
-            dense = np.zeros((len(lrows), d, d, len(rcols)))
-            for (r, c), op_id in set_once[s].items():
-                dense[rpos[r], :, :, cpos[c]] = self.ops.mats[op_id]
-            for (r, c), mat in trans[s].items():
-                dense[rpos[r], :, :, cpos[c]] += mat
+            m = mats[s]
+            if s > 0:
+                m.TransposeRows(order)
+            lvb = vb
+            if s < N - 1:
+                order, vb = self._sort_cols_by_qn(m, lvb, ops)
+            d_in, d_out = self.pb_in[s].dim, self.pb_out[s].dim
+            dense = np.zeros((m.rows, d_in, d_out, m.cols))
+            for x in range(m.rows):
+                for y, elem in m.row_items(x):
+                    op = elem.Realize(coefs, dense_ops)
+                    nz = op != 0.0
+                    dense[x, :, :, y][nz] = op[nz]
             if s == 0:
-                idx = [self.pb_in[0], bond_index[0], self.pb_out[0]]
-                arr = dense[0].transpose(0, 2, 1)          # (p_in, r, p_out)
+                idx = [self.pb_in[0], vb, self.pb_out[0]]
+                arr = dense[0].transpose(0, 2, 1)            # (p_in, r, p_out)
             elif s == N - 1:
-                idx = [self.pb_in[s], bond_index[s - 1].inverse(), self.pb_out[s]]
-                arr = dense[:, :, :, 0].transpose(1, 0, 2)  # (p_in, l, p_out)
+                idx = [self.pb_in[s], lvb.inverse(), self.pb_out[s]]
+                arr = dense[:, :, :, 0].transpose(1, 0, 2)    # (p_in, l, p_out)
             else:
-                idx = [bond_index[s - 1].inverse(), self.pb_in[s], self.pb_out[s], bond_index[s]]
+                idx = [lvb.inverse(), self.pb_in[s], self.pb_out[s], vb]
                 arr = dense
             mpo.append(_dense_to_blocks(arr, idx, zero))
-        self.bond_dims = [ix.dim for ix in bond_index]
         return mpo
 
 
