@@ -159,6 +159,16 @@ class FiniteMPS:
     def GetSitesInfo(self) -> SiteVec:
         return self.site_vec
 
+    def LoadTen(self, i: int, file: str) -> None:
+        """``TenVec::LoadTen`` (``ten_vec.h:50-55``)."""
+        self.tens[i] = read_tensor(file)
+
+    def DumpTen(self, i: int, file: str, release_mem: bool = False) -> None:
+        """``TenVec::DumpTen`` (``ten_vec.h:63-85``)."""
+        write_tensor(self[i], file)
+        if release_mem:
+            self.tens[i] = None
+
     def Dump(self, mps_path: str = kMpsPath, release_mem: bool = False) -> None:
         os.makedirs(mps_path, exist_ok=True)
         for i, t in enumerate(self.tens):

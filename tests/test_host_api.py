@@ -47,3 +47,69 @@ def test_batched_workload_definition():
     assert all(0.5 <= d <= 1.5 for _, d, _ in cases)
     assert {D for _, _, D in cases} <= {64, 128, 256, 512}
     assert cases == bench.batched_instances(64)   # seeded
+
+
+def _is_id_op(t):
+    """``test_site_vec.cc:22-39``: rank 2, square, (IN, OUT) legs that are
+    each other's inverse, identity elements."""
+    import numpy as np
+    from mps2_gb300.tensor import IN
+    assert len(t.indices) == 2 and t.indices[0].dim == t.indices[1].dim
+    assert t.indices[0].dir == IN and t.indices[0].inverse() == t.indices[1]
+    assert np.array_equal(t.to_dense(), np.eye(t.indices[0].dim))
+
+
+def test_site_vec_basic_features():
+    """``test_site_vec.cc:78-101``: the same local spaces, uniform and mixed."""
+    from mps2_gb300.site_vec import SiteVec
+    from mps2_gb300.tensor import Index, OUT
+    pb_out1 = Index([((0,), 1), ((1,), 1)], OUT)
+    pb_out2 = Index([((1,), 3)], OUT)
+    pb_in1, pb_in2 = pb_out1.inverse(), pb_out2.inverse()
+    for n, pb in ((1, pb_out1), (1, pb_in1), (3, pb_out1), (3, pb_in1)):
+        sv = SiteVec(n, pb)
+        assert sv.size == n and sv.sites == [pb_out1] * n
+        for op in sv.id_ops:
+            _is_id_op(op)
+    for spaces in ([pb_out1], [pb_out2, pb_out2], [pb_out1, pb_out2, pb_out1],
+                   [pb_in2, pb_out1, pb_out1, pb_in1, pb_out2]):
+        sv = SiteVec(spaces)
+        assert sv.size == len(spaces)
+        for s, ix in zip(sv.sites, spaces):
+            assert s == (ix if ix.dir == OUT else ix.inverse())
+        for op in sv.id_ops:
+            _is_id_op(op)
+
+
+def test_ten_vec_io(tmp_path):
+    """``test_ten_vec.cc:27-60`` on the MPS container: dump three tensors
+    (one with release), deallocate, load them back permuted."""
+    import numpy as np
+    from mps2_gb300.finite_mps import FiniteMPS
+    from mps2_gb300.site_vec import SiteVec
+    from mps2_gb300.tensor import GQTensor, Index, OUT
+    rng = np.random.default_rng(2)
+    idx_out = Index([((0,), 2), ((1,), 2)], OUT)
+    idx_in = idx_out.inverse()
+
+    def rand(div):
+        t = GQTensor([idx_in, idx_out], (div,))
+        for c in t.allowed_coords((div,)):
+            t.blocks[c] = rng.standard_normal(t.block_shape(c))
+        return t
+    tens = [rand(0), rand(1), rand(-1)]
+    v = FiniteMPS(SiteVec(3, idx_out))
+    for i, t in enumerate(tens):
+        v[i] = t
+    names = [str(tmp_path / f"ten{i}.gqten") for i in range(3)]
+    v.DumpTen(0, names[0])
+    v.DumpTen(1, names[1], True)
+    v.DumpTen(2, names[2], False)
+    v.dealloc(0)
+    v.dealloc(2)
+    assert v.empty()
+    v.LoadTen(0, names[2])
+    v.LoadTen(1, names[0])
+    v.LoadTen(2, names[1])
+    for got, want in zip((v[0], v[1], v[2]), (tens[2], tens[0], tens[1])):
+        assert got.indices == want.indices and got.dense_equal(want)
