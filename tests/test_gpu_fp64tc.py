@@ -128,9 +128,16 @@ def test_fp64tc_matvec_matches_oracle(lib, where):
 def test_sweeps_in_fp64tc_and_split_forms_match_fp64(lib):
     """Heisenberg L=20, D=200, 4 sweeps, Lanczos 1e-9 (the reference's
     CPU-runnable configuration): the FP64-accurate tensor-core form tracks
-    the FP64 form's per-sweep energies to 1e-11 relative; the split form
+    the FP64 form's per-sweep energies to 1e-10 relative; the split form
     (3xTF32 matvec, FP64-accurate environments, energies taken as
-    FP64-accurate tensor-core Rayleigh quotients) ends within 1e-9."""
+    FP64-accurate tensor-core Rayleigh quotients) ends within 1e-9.
+
+    The run is still converging (the energy drops by ~2e-3 per sweep), so
+    each sweep's energy carries the Lanczos stopping tolerance (1e-9
+    absolute, ~1e-10 relative here): rounding-level differences between two
+    arithmetic forms move where the solves stop.  The first sweeps agree to
+    1e-13 or better; the products themselves are checked bit-exactly and to
+    1e-13 by the contraction and matvec tests above."""
     from mps2_gb300 import hamiltonians as H
     from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS
     from mps2_gb300.vmps import DMRGState, LanczosParams, SweepParams, profile_enable, profile_read
@@ -150,7 +157,7 @@ def test_sweeps_in_fp64tc_and_split_forms_match_fp64(lib):
         profile_enable(False)
     print(energies)
     for e64, e in zip(energies["fp64"], energies["fp64tc"]):
-        assert abs(e - e64) / abs(e64) <= 1e-11
+        assert abs(e - e64) / abs(e64) <= 1e-10
     assert abs(energies["tf32x3"][-1] - energies["fp64"][-1]) / abs(energies["fp64"][-1]) <= 1e-9
 
 
