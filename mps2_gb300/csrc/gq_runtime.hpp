@@ -23,6 +23,15 @@ struct Lane {
   void *cublas = nullptr;          // cublasHandle_t, created lazily
   char *staging = nullptr;         // pinned ring for work-list uploads
   size_t staging_head = 0;
+  // Auxiliary streams for independent library calls inside one operation
+  // (the block SVD's eigensolves of different sizes run side by side),
+  // forked from and joined back to `stream` with events; created on first
+  // use by init_aux.
+  static constexpr int kAux = 3;
+  cudaStream_t aux_stream[kAux] = {};
+  void *aux_cusolver[kAux] = {};  // cusolverDnHandle_t on aux_stream[i]
+  cudaEvent_t fork_event = nullptr;
+  cudaEvent_t join_event[kAux] = {};
 };
 
 struct Context {
@@ -34,6 +43,9 @@ struct Context {
 Context &ctx();
 void init_context(int device);
 void init_lane(Lane &l);
+void init_aux(Lane &l);               // the lane's auxiliary streams and events
+void fork_aux(Lane &l, int n);        // aux streams 0..n-1 wait for `stream`
+void join_aux(Lane &l, int n);        // `stream` waits for aux streams 0..n-1
 void destroy_lane_handles(Lane &l);  // cuSOLVER / cuBLAS handles (svd.cu)
 Lane &lane();              // this thread's lane
 Lane *lane_create();       // a new lane (own non-blocking stream)

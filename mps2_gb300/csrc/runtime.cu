@@ -58,6 +58,29 @@ void init_lane(Lane &l) {
   GQ_CUDA(cudaStreamSynchronize(l.stream));
 }
 
+void init_aux(Lane &l) {
+  if (l.fork_event) return;
+  for (int i = 0; i < Lane::kAux; ++i) {
+    GQ_CUDA(cudaStreamCreateWithFlags(&l.aux_stream[i], cudaStreamNonBlocking));
+    GQ_CUDA(cudaEventCreateWithFlags(&l.join_event[i], cudaEventDisableTiming));
+  }
+  GQ_CUDA(cudaEventCreateWithFlags(&l.fork_event, cudaEventDisableTiming));
+}
+
+void fork_aux(Lane &l, int n) {
+  if (n <= 0) return;
+  init_aux(l);
+  GQ_CUDA(cudaEventRecord(l.fork_event, l.stream));
+  for (int i = 0; i < n; ++i) GQ_CUDA(cudaStreamWaitEvent(l.aux_stream[i], l.fork_event, 0));
+}
+
+void join_aux(Lane &l, int n) {
+  for (int i = 0; i < n; ++i) {
+    GQ_CUDA(cudaEventRecord(l.join_event[i], l.aux_stream[i]));
+    GQ_CUDA(cudaStreamWaitEvent(l.stream, l.join_event[i], 0));
+  }
+}
+
 Lane &lane() { return t_lane ? *t_lane : ctx().main; }
 
 Lane *lane_create() {
@@ -71,11 +94,19 @@ void lane_destroy(Lane *l) {
   if (!l) return;
   if (t_lane == l) t_lane = nullptr;
   cudaStreamSynchronize(l->stream);
-  if (l->cusolver || l->cublas) destroy_lane_handles(*l);
+  destroy_lane_handles(*l);
   cudaFreeAsync(l->dev_scalars, l->stream);
   cudaStreamSynchronize(l->stream);
   cudaFreeHost(l->host_scalars);
   if (l->staging) cudaFreeHost(l->staging);
+  if (l->fork_event) {
+    for (int i = 0; i < Lane::kAux; ++i) {
+      cudaStreamSynchronize(l->aux_stream[i]);
+      cudaStreamDestroy(l->aux_stream[i]);
+      cudaEventDestroy(l->join_event[i]);
+    }
+    cudaEventDestroy(l->fork_event);
+  }
   cudaStreamDestroy(l->stream);
   delete l;
 }

@@ -85,6 +85,19 @@ cusolverDnHandle_t solver() {
   return (cusolverDnHandle_t)l.cusolver;
 }
 
+// cuSOLVER handle on the lane's auxiliary stream i.
+cusolverDnHandle_t aux_solver(int i) {
+  auto &l = lane();
+  init_aux(l);
+  if (!l.aux_cusolver[i]) {
+    cusolverDnHandle_t h;
+    GQ_SOLVER(cusolverDnCreate(&h));
+    GQ_SOLVER(cusolverDnSetStream(h, l.aux_stream[i]));
+    l.aux_cusolver[i] = h;
+  }
+  return (cusolverDnHandle_t)l.aux_cusolver[i];
+}
+
 cublasHandle_t blas() {
   auto &l = lane();
   if (!l.cublas) {
@@ -390,6 +403,10 @@ void destroy_lane_handles(Lane &l) {
   if (l.cusolver) cusolverDnDestroy((cusolverDnHandle_t)l.cusolver);
   if (l.cublas) cublasDestroy((cublasHandle_t)l.cublas);
   l.cusolver = l.cublas = nullptr;
+  for (auto &a : l.aux_cusolver) {
+    if (a) cusolverDnDestroy((cusolverDnHandle_t)a);
+    a = nullptr;
+  }
 }
 
 SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_err,
@@ -619,32 +636,59 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
                               ev.p + g->ev_off, bs));
         }
       }
-    cusolverDnParams_t sp;
-    GQ_SOLVER(cusolverDnCreateParams(&sp));
-    size_t dws = 0, hws = 0;
-    for (auto &kv : buckets) {
-      const int64_t bs = kv.first, nb = (int64_t)kv.second.size();
+    // One batched eigensolve per bucket.  The solves are latency-bound (a
+    // 1486-row syevd is ~60 ms of small launches), so buckets of different
+    // sizes run side by side: largest first, dealt round-robin over the
+    // lane's stream and its auxiliary streams, each with its own handle and
+    // workspace, joined back before the values are read.  Same calls on the
+    // same data as one after another.
+    struct Solve {
+      int64_t bs, nb, io;
+      Group *first;
+      int slot;
+    };
+    std::vector<Solve> solves;
+    {
+      int64_t io = 0;  // info words in bucket (map) order
+      for (auto &kv : buckets) {
+        solves.push_back({kv.first, (int64_t)kv.second.size(), io, kv.second[0], 0});
+        io += (int64_t)kv.second.size();
+      }
+    }
+    std::stable_sort(solves.begin(), solves.end(),
+                     [](const Solve &a, const Solve &b) { return a.bs > b.bs; });
+    const int nslot = (int)std::min<size_t>(solves.size(), 1 + Lane::kAux);
+    for (size_t k = 0; k < solves.size(); ++k) solves[k].slot = (int)(k % nslot);
+    auto handle_of = [&](int slot) { return slot == 0 ? h : aux_solver(slot - 1); };
+    std::vector<cusolverDnParams_t> sp(nslot);
+    for (auto &x : sp) GQ_SOLVER(cusolverDnCreateParams(&x));
+    std::vector<size_t> dws(nslot, 0), hws(nslot, 0);
+    for (const Solve &v : solves) {
       size_t d1 = 0, h1 = 0;
       GQ_SOLVER(cusolverDnXsyevBatched_bufferSize(
-          h, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, bs, CUDA_R_64F,
-          ev.p + kv.second[0]->ev_off, bs, CUDA_R_64F, w.p + kv.second[0]->w_off, CUDA_R_64F, &d1,
-          &h1, nb));
-      dws = std::max(dws, d1);
-      hws = std::max(hws, h1);
+          handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
+          CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off, CUDA_R_64F,
+          &d1, &h1, v.nb));
+      dws[v.slot] = std::max(dws[v.slot], d1);
+      hws[v.slot] = std::max(hws[v.slot], h1);
     }
-    DevBuf dwork((int64_t)(dws / sizeof(double)) + 2);
-    std::vector<char> hwork(hws + 16);
+    std::vector<DevBuf> dwork;
+    std::vector<std::vector<char>> hwork;
+    for (int k = 0; k < nslot; ++k) {
+      dwork.emplace_back((int64_t)(dws[k] / sizeof(double)) + 2);
+      hwork.emplace_back(hws[k] + 16);
+    }
     einfo.upload(std::vector<int>(n_gram, 0));
-    int64_t io = 0;
-    for (auto &kv : buckets) {
-      const int64_t bs = kv.first, nb = (int64_t)kv.second.size();
-      GQ_SOLVER(cusolverDnXsyevBatched(h, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, bs,
-                                       CUDA_R_64F, ev.p + kv.second[0]->ev_off, bs, CUDA_R_64F,
-                                       w.p + kv.second[0]->w_off, CUDA_R_64F, dwork.p, dws,
-                                       hwork.data(), hws, einfo.p + io, nb));
-      io += nb;
-    }
-    cusolverDnDestroyParams(sp);
+    Lane &ln = lane();
+    fork_aux(ln, nslot - 1);  // after the Gram matrices, workspaces and info words
+    for (const Solve &v : solves)
+      GQ_SOLVER(cusolverDnXsyevBatched(
+          handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
+          CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off, CUDA_R_64F,
+          dwork[v.slot].p, dws[v.slot], hwork[v.slot].data(), hws[v.slot], einfo.p + v.io,
+          v.nb));
+    join_aux(ln, nslot - 1);  // the lane's stream waits for every solve
+    for (auto &x : sp) cusolverDnDestroyParams(x);
   }
   prof_end(kProfSvdEig, 0.0, 0.0);
   // ---- values to the host ---------------------------------------------------
