@@ -46,6 +46,21 @@ void init_lane(Lane &l);
 void init_aux(Lane &l);               // the lane's auxiliary streams and events
 void fork_aux(Lane &l, int n);        // aux streams 0..n-1 wait for `stream`
 void join_aux(Lane &l, int n);        // `stream` waits for aux streams 0..n-1
+// Joins aux streams 0..n-1 back into the lane's stream when it goes out of
+// scope, on every path (errors are not thrown from the destructor).
+struct AuxJoin {
+  Lane &l;
+  int n;
+  AuxJoin(Lane &lane_, int n_) : l(lane_), n(n_) {}
+  AuxJoin(const AuxJoin &) = delete;
+  AuxJoin &operator=(const AuxJoin &) = delete;
+  ~AuxJoin() {
+    for (int i = 0; i < n; ++i) {
+      cudaEventRecord(l.join_event[i], l.aux_stream[i]);
+      cudaStreamWaitEvent(l.stream, l.join_event[i], 0);
+    }
+  }
+};
 void destroy_lane_handles(Lane &l);  // cuSOLVER / cuBLAS handles (svd.cu)
 Lane &lane();              // this thread's lane
 Lane *lane_create();       // a new lane (own non-blocking stream)

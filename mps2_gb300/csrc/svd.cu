@@ -681,13 +681,18 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     einfo.upload(std::vector<int>(n_gram, 0));
     Lane &ln = lane();
     fork_aux(ln, nslot - 1);  // after the Gram matrices, workspaces and info words
-    for (const Solve &v : solves)
-      GQ_SOLVER(cusolverDnXsyevBatched(
-          handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
-          CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off, CUDA_R_64F,
-          dwork[v.slot].p, dws[v.slot], hwork[v.slot].data(), hws[v.slot], einfo.p + v.io,
-          v.nb));
-    join_aux(ln, nslot - 1);  // the lane's stream waits for every solve
+    {
+      // the lane's stream waits for every solve before anything here is
+      // released -- on an error too, since the workspaces are freed in
+      // stream order on the lane's stream
+      AuxJoin joined(ln, nslot - 1);
+      for (const Solve &v : solves)
+        GQ_SOLVER(cusolverDnXsyevBatched(
+            handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
+            CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off,
+            CUDA_R_64F, dwork[v.slot].p, dws[v.slot], hwork[v.slot].data(), hws[v.slot],
+            einfo.p + v.io, v.nb));
+    }
     for (auto &x : sp) cusolverDnDestroyParams(x);
   }
   prof_end(kProfSvdEig, 0.0, 0.0);
