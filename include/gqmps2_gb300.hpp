@@ -10,6 +10,7 @@
  *   TenVec / MPO (ten_vec.h:30-85, mpo.h:25)       gqmps2::TenVec, gqmps2::MPO
  *   FiniteMPS (finite_mps.h:51-140, mps.h:69-107)  gqmps2::FiniteMPS
  *   DirectStateInitMps (finite_mps_init.h:216)     gqmps2::DirectStateInitMps
+ *   TruncateMPS (finite_mps.h:251-300)             gqmps2::TruncateMPS
  *   TwoSiteFiniteVMPS (..._vmps_impl.h:77-101)     gqmps2::TwoSiteFiniteVMPS
  *   LanczosSolver / LanczosRes (lanczos_solver_impl.h:71-226)
  *                                                  gqmps2::LanczosSolver / LanczosRes
@@ -548,6 +549,34 @@ class FiniteMPS : public TenVec<GQTensor> {
  private:
   SiteVec site_vec_;
 };
+
+/* TruncateMPS (finite_mps.h:251-300) on the GPU: centralise at 0, normalise
+ * the head, then one truncating SVD per bond from the left.  Every site must
+ * be loaded.  Optionally returns each bond's truncation error and dimension
+ * (the reference prints them). */
+inline void TruncateMPS(FiniteMPS &mps, double trunc_err, size_t Dmin, size_t Dmax,
+                        std::vector<double> *errs = nullptr,
+                        std::vector<int64_t> *dims = nullptr) {
+  const int n = (int)mps.size();
+  if (n < 2) throw Error("TruncateMPS: at least two sites");
+  std::vector<DeviceTensor> d;
+  std::vector<gq_tensor *> h;
+  for (int i = 0; i < n; ++i) {
+    d.push_back(DeviceTensor::FromHost(mps[i]));
+    h.push_back(d.back().get());
+  }
+  std::vector<int> cano(mps.tens_cano_type_.begin(), mps.tens_cano_type_.end());
+  std::vector<double> e(n - 1);
+  std::vector<int64_t> D(n - 1);
+  Check(gq_mps_truncate(h.data(), n, cano.data(), trunc_err, (int64_t)Dmin, (int64_t)Dmax,
+                        e.data(), D.data()));
+  for (int i = 0; i < n; ++i) {  // the handles' tensors were rewritten in place
+    mps[i] = d[i].ToHost();
+    mps.tens_cano_type_[i] = (MPSTenCanoType)cano[i];
+  }
+  if (errs) *errs = e;
+  if (dims) *dims = D;
+}
 
 /* finite_mps_init.h:216-262: bond-dimension-1 product state; the result is
  * already right-canonical (what the reference's trailing Centralize(0)

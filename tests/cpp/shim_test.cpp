@@ -110,6 +110,19 @@ int run_host(const std::string &dir) {
   tv.LoadTen(2, dir + "/ten1.gqten");
   expect(tv[0] == t2 && tv[1] == t0 && tv[2] == t1, "TenVec load after dump");
 
+  // test_duovector.cc: copies own their elements, moves take them over
+  TenVec<GQTensor> copy(tv);
+  expect(copy.size() == 3 && copy[0] == tv[0] && copy(0) != tv(0), "TenVec copy is deep");
+  const GQTensor *p0 = tv(0);
+  TenVec<GQTensor> moved(std::move(tv));
+  expect(moved(0) == p0 && moved[0] == copy[0], "TenVec move keeps the elements");
+  TenVec<GQTensor> assigned(1);
+  assigned = copy;
+  expect(assigned.size() == 3 && assigned[2] == copy[2] && assigned(2) != copy(2),
+         "TenVec copy assignment is deep");
+  assigned.dealloc(1);
+  expect(assigned(1) == nullptr && assigned(0) != nullptr, "TenVec dealloc of one element");
+
   bool threw = false;
   try {
     GQTensor bad;
@@ -186,6 +199,22 @@ int run_dmrg(const std::string &dir) {
         worst = std::fmax(worst, std::fabs(m.GetElem({x, y}) - (x == y ? 1.0 : 0.0)));
   }
   std::printf("left_canonical_err %.3g\n", worst);
+
+  // TruncateMPS to D = 2: every bond at most 2, the state stays normalised
+  {
+    FiniteMPS tm = dmps;
+    std::vector<double> errs;
+    std::vector<int64_t> dims;
+    TruncateMPS(tm, 0.0, 1, 2, &errs, &dims);
+    int64_t dmax_seen = 0;
+    for (auto x : dims) dmax_seen = x > dmax_seen ? x : dmax_seen;
+    std::printf("truncate_dmax %lld\n", (long long)dmax_seen);
+    std::printf("truncate_bonds %zu\n", dims.size());
+    double nrm = 0.0;  // <psi|psi> from the left-canonical tensors: |A_{N-1}|^2
+    for (auto &b : tm[N - 1].Blocks())
+      for (double v : b.second) nrm += v * v;
+    std::printf("truncate_norm %.17g\n", nrm);
+  }
 
   // the split form, one sweep from the converged state (right-canonical again)
   dmps.Centralize(0);

@@ -3,8 +3,8 @@ g++ against the library: its host parts on the CPU (tensor files shared with
 the Python side, ``DirectStateInitMps``, ``SiteVec``, ``TenVec``), and on the
 GPU the reference's 1DHeisenberg DMRG case restated in C++
 (``test_two_site_update_finite_vmps.cc:186-220``: golden energy
--2.493577133888 to 1e-12, then a resumed call), a ``LanczosSolver`` and
-``FiniteMPS::Centralize`` through the same header."""
+-2.493577133888 to 1e-12, then a resumed call), a ``LanczosSolver``,
+``FiniteMPS::Centralize`` and ``TruncateMPS`` through the same header."""
 import os
 import subprocess
 
@@ -82,5 +82,10 @@ def test_cpp_shim_dmrg(shim_exe, tmp_path):
     assert vals["center"] == "3"
     assert vals["cano"].split() == ["1", "1", "1", "0", "2", "2"]
     assert float(vals["left_canonical_err"]) <= 1e-13
+    # TruncateMPS to D = 2 (test_finite_mps.cc: every bond within Dmax, the
+    # state normalised)
+    assert int(vals["truncate_bonds"]) == 5
+    assert int(vals["truncate_dmax"]) == 2
+    assert abs(float(vals["truncate_norm"]) - 1.0) <= 1e-12
     # split form: 3xTF32 products, FP64-accurate energy; 1e-9 relative
     assert abs(float(vals["e0_split"]) - GOLDEN_1D_HEISENBERG) <= 1e-9 * abs(GOLDEN_1D_HEISENBERG)
