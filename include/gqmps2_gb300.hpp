@@ -11,6 +11,8 @@
  *   FiniteMPS (finite_mps.h:51-140, mps.h:69-107)  gqmps2::FiniteMPS
  *   DirectStateInitMps (finite_mps_init.h:216)     gqmps2::DirectStateInitMps
  *   TruncateMPS (finite_mps.h:251-300)             gqmps2::TruncateMPS
+ *   MeasureOneSiteOp / MeasureTwoSiteOp / MeasureMultiSiteOp / DumpMeasuRes
+ *     (finite_mps_measu.h:150-584)                 same names
  *   TwoSiteFiniteVMPS (..._vmps_impl.h:77-101)     gqmps2::TwoSiteFiniteVMPS
  *   LanczosSolver / LanczosRes (lanczos_solver_impl.h:71-226)
  *                                                  gqmps2::LanczosSolver / LanczosRes
@@ -655,6 +657,287 @@ struct SweepParams {
     return p;
   }
 };
+
+/* ---------------------------------------------------------------------- */
+/* measurement (finite_mps_measu.h:150-584)                                */
+/* ---------------------------------------------------------------------- */
+struct MeasuResElem {
+  std::vector<size_t> sites;
+  double avg = 0.0;
+};
+using MeasuRes = std::vector<MeasuResElem>;
+using MeasuResSet = std::vector<MeasuRes>;
+
+/* DumpMeasuRes (:556-584): "[\n  [[i, j], avg],\n  ...]" in <basename>.json,
+ * averages with 12 significant digits in a 14-wide field. */
+inline void DumpMeasuRes(const MeasuRes &res, const std::string &basename) {
+  std::FILE *f = std::fopen((basename + ".json").c_str(), "w");
+  if (!f) throw Error("cannot write " + basename + ".json");
+  std::fputs("[\n", f);
+  for (size_t n = 0; n < res.size(); ++n) {
+    std::fputs("  [[", f);
+    for (size_t k = 0; k < res[n].sites.size(); ++k)
+      std::fprintf(f, k ? ", %zu" : "%zu", res[n].sites[k]);
+    std::fprintf(f, "], %14.12g", res[n].avg);
+    std::fputs(n + 1 == res.size() ? "]\n" : "],\n", f);
+  }
+  std::fputs("]", f);
+  std::fclose(f);
+}
+
+namespace measu_detail {
+
+inline DeviceTensor Contract(const DeviceTensor &a, const DeviceTensor &b,
+                             const std::vector<int> &xa, const std::vector<int> &xb) {
+  gq_tensor *c = nullptr;
+  double flops = 0.0;
+  Check(gq_contract(a.get(), b.get(), (int)xa.size(), xa.data(), xb.data(), GQ_PREC_FP64, &c,
+                    &flops));
+  return DeviceTensor(c);
+}
+
+inline DeviceTensor Dag(const DeviceTensor &a) {
+  gq_tensor *c = nullptr;
+  Check(gq_tensor_dag(a.get(), &c));
+  return DeviceTensor(c);
+}
+
+/* every leg of a (in order xa) against every leg of b (in order xb), on the
+ * host: the last contraction of each event reduces two site-sized tensors to
+ * one number */
+inline double FullContract(const GQTensor &a, const GQTensor &b, const std::vector<int> &xa,
+                           const std::vector<int> &xb) {
+  const size_t r = a.Rank();
+  if (b.Rank() != r || xa.size() != r || xb.size() != r)
+    throw Error("full contraction: every leg must be contracted");
+  double acc = 0.0;
+  for (auto &ba : a.Blocks()) {
+    GQTensor::Coords cb(r);
+    for (size_t k = 0; k < r; ++k) cb[xb[k]] = ba.first[xa[k]];
+    auto it = b.Blocks().find(cb);
+    if (it == b.Blocks().end()) continue;
+    const auto sa = a.BlockShape(ba.first), sb = b.BlockShape(cb);
+    std::vector<int64_t> strb(r, 1), step(r, 0);  // b's stride along each of a's legs
+    for (int j = (int)r - 2; j >= 0; --j) strb[j] = strb[j + 1] * sb[j + 1];
+    for (size_t k = 0; k < r; ++k) step[xa[k]] = strb[xb[k]];
+    std::vector<int64_t> idx(r, 0);
+    int64_t ob = 0;
+    for (double va : ba.second) {  // a's elements in row-major order
+      acc += va * it->second[ob];
+      for (int l = (int)r - 1; l >= 0; --l) {  // odometer over a's legs
+        if (++idx[l] < sa[l]) {
+          ob += step[l];
+          break;
+        }
+        ob -= step[l] * (sa[l] - 1);
+        idx[l] = 0;
+      }
+    }
+  }
+  return acc;
+}
+
+/* the MPS on the device with the reference's canonical-type bookkeeping */
+struct DeviceMPS {
+  explicit DeviceMPS(FiniteMPS &m) : host(m), n((int)m.size()) {
+    for (int i = 0; i < n; ++i) t.push_back(DeviceTensor::FromHost(m[i]));
+    cano.assign(m.tens_cano_type_.begin(), m.tens_cano_type_.end());
+  }
+  void Centralize(int c) {
+    std::vector<gq_tensor *> h;
+    for (auto &x : t) h.push_back(x.get());
+    Check(gq_mps_centralize(h.data(), n, c, cano.data()));
+    center = c;
+  }
+  void WriteBack() {
+    for (int i = 0; i < n; ++i) {
+      host[i] = t[i].ToHost();
+      host.tens_cano_type_[i] = (MPSTenCanoType)cano[i];
+    }
+    host.center_ = center;
+  }
+  FiniteMPS &host;
+  int n;
+  std::vector<DeviceTensor> t;
+  std::vector<int> cano;
+  long center = -1;
+};
+
+/* OneSiteOpAvg (:366-402) */
+inline double OneSiteOpAvg(const DeviceTensor &cent, const DeviceTensor &op, int site, int n) {
+  std::vector<int> x1, y1{0}, x2, y2;
+  if (site == 0) {
+    x1 = {0}; x2 = {0, 1}; y2 = {1, 0};
+  } else if (site == n - 1) {
+    x1 = {1}; x2 = {0, 1}; y2 = {0, 1};
+  } else {
+    x1 = {1}; x2 = {0, 2, 1}; y2 = {0, 1, 2};
+  }
+  DeviceTensor temp = Contract(cent, op, x1, y1);
+  return FullContract(temp.ToHost(), Dag(cent).ToHost(), x2, y2);
+}
+
+/* CtrctMidTen (:528-554) */
+inline DeviceTensor CtrctMidTen(DeviceMPS &dm, int site, const GQTensor &op,
+                                const GQTensor &id_op, const DeviceTensor &t) {
+  const DeviceTensor &a = dm.t[site];
+  if (op == id_op) {
+    DeviceTensor temp = Contract(a, t, {0}, {0});
+    return Contract(temp, Dag(a), {0, 2}, {1, 0});
+  }
+  DeviceTensor temp1 = Contract(a, t, {0}, {0});
+  DeviceTensor temp2 = Contract(temp1, DeviceTensor::FromHost(op), {0}, {0});
+  return Contract(temp2, Dag(a), {1, 2}, {0, 1});
+}
+
+/* OpsVecAvg (:462-526): the MPS is centralised at `head` */
+inline double OpsVecAvg(DeviceMPS &dm, const std::vector<GQTensor> &ops, int head, int tail) {
+  if ((int)ops.size() != tail - head + 1) throw Error("measurement: one operator per site");
+  const auto &id_ops = dm.host.GetSitesInfo().id_ops;
+  std::vector<int> a1, a2, a3;
+  if (head == 0) {
+    a1 = {0}; a2 = {1}; a3 = {0};
+  } else {
+    a1 = {1}; a2 = {0, 2}; a3 = {0, 1};
+  }
+  const DeviceTensor &h = dm.t[head];
+  DeviceTensor temp0 = Contract(h, DeviceTensor::FromHost(ops[0]), a1, {0});
+  DeviceTensor t = Contract(temp0, Dag(h), a2, a3);
+  for (int i = head + 1; i < tail; ++i) t = CtrctMidTen(dm, i, ops[i - head], id_ops[i], t);
+  std::vector<int> b1, b2;
+  if (tail == dm.n - 1) {
+    b1 = {0, 1}; b2 = {0, 1};
+  } else {
+    b1 = {0, 1, 2}; b2 = {2, 0, 1};
+  }
+  const DeviceTensor &tl = dm.t[tail];
+  DeviceTensor temp2 = Contract(tl, t, {0}, {0});
+  DeviceTensor temp3 = Contract(temp2, DeviceTensor::FromHost(ops.back()), {0}, {0});
+  return FullContract(temp3.ToHost(), Dag(tl).ToHost(), b1, b2);
+}
+
+/* MultiSiteOpAvg (:404-437): A, inserts, B, inserts, ..., and an optional
+ * tail string after the last physical operator */
+inline MeasuResElem MultiSiteOpAvg(DeviceMPS &dm, const std::vector<GQTensor> &phys_ops,
+                                   const std::vector<std::vector<GQTensor>> &inst_ops_set,
+                                   const std::vector<size_t> &sites) {
+  const size_t ni = inst_ops_set.size(), np = phys_ops.size();
+  if (!(np == ni + 1 || np == ni)) throw Error("measurement: wrong number of insert lists");
+  std::vector<GQTensor> ops;
+  for (size_t i = 0; i + 1 < np; ++i) {
+    ops.push_back(phys_ops[i]);
+    ops.insert(ops.end(), inst_ops_set[i].begin(), inst_ops_set[i].end());
+  }
+  ops.push_back(phys_ops.back());
+  if (ni == np) ops.insert(ops.end(), inst_ops_set.back().begin(), inst_ops_set.back().end());
+  const int head = (int)sites[0];
+  const int tail = head + (int)ops.size() - 1;
+  return MeasuResElem{sites, OpsVecAvg(dm, ops, head, tail)};
+}
+
+inline void CheckSites(const std::vector<size_t> &sites) {
+  if (sites.size() < 2) throw Error("measurement: at least two sites per event");
+  for (size_t k = 1; k < sites.size(); ++k)
+    if (sites[k] < sites[k - 1]) throw Error("measurement: sites must be ascending");
+}
+
+}  // namespace measu_detail
+
+/* MeasureOneSiteOp (:150-214), a list of operators: one result per operator
+ * and site; the MPS ends centralised at its last site. */
+inline MeasuResSet MeasureOneSiteOp(FiniteMPS &mps, const std::vector<GQTensor> &ops,
+                                    const std::vector<std::string> &res_file_basenames) {
+  if (ops.size() != res_file_basenames.size())
+    throw Error("MeasureOneSiteOp: one file name per operator");
+  measu_detail::DeviceMPS dm(mps);
+  std::vector<DeviceTensor> dops;
+  for (auto &o : ops) dops.push_back(DeviceTensor::FromHost(o));
+  MeasuResSet res(ops.size(), MeasuRes(dm.n));
+  for (int i = 0; i < dm.n; ++i) {
+    dm.Centralize(i);
+    for (size_t j = 0; j < ops.size(); ++j)
+      res[j][i] = MeasuResElem{{(size_t)i}, measu_detail::OneSiteOpAvg(dm.t[i], dops[j], i, dm.n)};
+  }
+  dm.WriteBack();
+  for (size_t j = 0; j < ops.size(); ++j) DumpMeasuRes(res[j], res_file_basenames[j]);
+  return res;
+}
+
+inline MeasuRes MeasureOneSiteOp(FiniteMPS &mps, const GQTensor &op,
+                                 const std::string &res_file_basename) {
+  return MeasureOneSiteOp(mps, std::vector<GQTensor>{op},
+                          std::vector<std::string>{res_file_basename})[0];
+}
+
+/* MeasureMultiSiteOp (:300-340): inst_ops_set[e][g] lists the insert
+ * operators of gap g of event e. */
+inline MeasuRes MeasureMultiSiteOp(FiniteMPS &mps,
+                                   const std::vector<std::vector<GQTensor>> &phys_ops_set,
+                                   const std::vector<std::vector<std::vector<GQTensor>>> &inst_ops_set,
+                                   const std::vector<std::vector<size_t>> &sites_set,
+                                   const std::string &res_file_basename) {
+  if (phys_ops_set.size() != sites_set.size() || inst_ops_set.size() != sites_set.size())
+    throw Error("MeasureMultiSiteOp: one operator list per event");
+  measu_detail::DeviceMPS dm(mps);
+  MeasuRes res;
+  for (size_t e = 0; e < sites_set.size(); ++e) {
+    measu_detail::CheckSites(sites_set[e]);
+    dm.Centralize((int)sites_set[e][0]);
+    res.push_back(measu_detail::MultiSiteOpAvg(dm, phys_ops_set[e], inst_ops_set[e], sites_set[e]));
+  }
+  dm.WriteBack();
+  DumpMeasuRes(res, res_file_basename);
+  return res;
+}
+
+/* MeasureMultiSiteOp (:342-364): one insert operator repeated across each gap */
+inline MeasuRes MeasureMultiSiteOp(FiniteMPS &mps,
+                                   const std::vector<std::vector<GQTensor>> &phys_ops_set,
+                                   const std::vector<std::vector<GQTensor>> &inst_ops_set,
+                                   const std::vector<std::vector<size_t>> &sites_set,
+                                   const std::string &res_file_basename) {
+  std::vector<std::vector<std::vector<GQTensor>>> full;
+  for (size_t e = 0; e < sites_set.size(); ++e) {
+    measu_detail::CheckSites(sites_set[e]);
+    if (phys_ops_set.at(e).size() != inst_ops_set.at(e).size() + 1)
+      throw Error("MeasureMultiSiteOp: one insert operator per gap");
+    std::vector<std::vector<GQTensor>> gaps;
+    for (size_t g = 0; g < inst_ops_set[e].size(); ++g)
+      gaps.emplace_back(sites_set[e][g + 1] - sites_set[e][g] - 1, inst_ops_set[e][g]);
+    full.push_back(std::move(gaps));
+  }
+  return MeasureMultiSiteOp(mps, phys_ops_set, full, sites_set, res_file_basename);
+}
+
+/* MeasureTwoSiteOp (:216-259): <A_i O ... O B_j> with its own list of insert
+ * operators for each event */
+inline MeasuRes MeasureTwoSiteOp(FiniteMPS &mps, const std::vector<GQTensor> &phys_ops,
+                                 const std::vector<std::vector<GQTensor>> &inst_ops_set,
+                                 const std::vector<std::vector<size_t>> &sites_set,
+                                 const std::string &res_file_basename) {
+  if (phys_ops.size() != 2) throw Error("MeasureTwoSiteOp: two physical operators");
+  if (inst_ops_set.size() != sites_set.size())
+    throw Error("MeasureTwoSiteOp: one insert list per event");
+  std::vector<std::vector<GQTensor>> phys(sites_set.size(), phys_ops);
+  std::vector<std::vector<std::vector<GQTensor>>> inst;
+  for (size_t e = 0; e < sites_set.size(); ++e) {
+    if (sites_set[e].size() != 2 || sites_set[e][1] - sites_set[e][0] - 1 != inst_ops_set[e].size())
+      throw Error("MeasureTwoSiteOp: one insert operator per site between the pair");
+    inst.push_back({inst_ops_set[e]});
+  }
+  return MeasureMultiSiteOp(mps, phys, inst, sites_set, res_file_basename);
+}
+
+/* MeasureTwoSiteOp (:261-298): the same insert operator on every site between */
+inline MeasuRes MeasureTwoSiteOp(FiniteMPS &mps, const std::vector<GQTensor> &phys_ops,
+                                 const GQTensor &inst_op,
+                                 const std::vector<std::vector<size_t>> &sites_set,
+                                 const std::string &res_file_basename) {
+  if (phys_ops.size() != 2) throw Error("MeasureTwoSiteOp: two physical operators");
+  std::vector<std::vector<GQTensor>> phys(sites_set.size(), phys_ops);
+  std::vector<std::vector<GQTensor>> inst(sites_set.size(), std::vector<GQTensor>{inst_op});
+  return MeasureMultiSiteOp(mps, phys, inst, sites_set, res_file_basename);
+}
 
 /* ---------------------------------------------------------------------- */
 /* the solver                                                              */

@@ -123,6 +123,37 @@ int run_host(const std::string &dir) {
   assigned.dealloc(1);
   expect(assigned(1) == nullptr && assigned(0) != nullptr, "TenVec dealloc of one element");
 
+  // the host-side full contraction of the measurements against an explicit
+  // element sum: a(i, j, k) b(k, i, j), legs matched a0-b1, a1-b2, a2-b0
+  {
+    Index p({QNSector({0}, 2), QNSector({1}, 3)}, OUT), q({QNSector({0}, 1), QNSector({1}, 2)}, OUT);
+    Index r({QNSector({0}, 2), QNSector({-1}, 2)}, IN);
+    unsigned st2 = 11;
+    auto rnd = [&] {
+      st2 = st2 * 1664525u + 1013904223u;
+      return (double)(st2 >> 8) / (double)(1u << 24) - 0.5;
+    };
+    GQTensor a({p, q, InverseIndex(r)}), b({r, InverseIndex(p), InverseIndex(q)});
+    for (int64_t i = 0; i < p.dim(); ++i)
+      for (int64_t j = 0; j < q.dim(); ++j)
+        for (int64_t k = 0; k < r.dim(); ++k) {
+          QN qa = a.BlockDiv({(int)p.CoorToSector(i).first, (int)q.CoorToSector(j).first,
+                              (int)r.CoorToSector(k).first});
+          if (qa == QN{1}) {
+            a.SetElem({i, j, k}, rnd());
+            b.SetElem({k, i, j}, rnd());
+          }
+        }
+    double want = 0.0;
+    for (int64_t i = 0; i < p.dim(); ++i)
+      for (int64_t j = 0; j < q.dim(); ++j)
+        for (int64_t k = 0; k < r.dim(); ++k) want += a.GetElem({i, j, k}) * b.GetElem({k, i, j});
+    double got = measu_detail::FullContract(a, b, {0, 1, 2}, {1, 2, 0});
+    expect(std::fabs(got - want) <= 1e-14 * (1.0 + std::fabs(want)), "full contraction");
+    MeasuRes mr{MeasuResElem{{0}, 0.25}, MeasuResElem{{1, 4}, -0.125}};
+    DumpMeasuRes(mr, dir + "/measu");
+  }
+
   bool threw = false;
   try {
     GQTensor bad;
@@ -199,6 +230,21 @@ int run_dmrg(const std::string &dir) {
         worst = std::fmax(worst, std::fabs(m.GetElem({x, y}) - (x == y ? 1.0 : 0.0)));
   }
   std::printf("left_canonical_err %.3g\n", worst);
+
+  // measurements on the converged state; the same MPS is dumped for the
+  // Python side to measure too
+  {
+    dmps.Dump(dir + "/mps_meas");
+    GQTensor sz({InverseIndex(spin_half_out()), spin_half_out()});
+    sz.SetElem({0, 0}, 0.5);
+    sz.SetElem({1, 1}, -0.5);
+    auto r1 = MeasureOneSiteOp(dmps, sz, dir + "/sz");
+    std::vector<std::vector<size_t>> pairs = {{0, 1}, {0, 3}, {2, 5}, {1, 4}};
+    auto r2 = MeasureTwoSiteOp(dmps, {sz, sz}, dsite_vec_6.id_ops[0], pairs, dir + "/szsz");
+    std::printf("meas_one %zu\n", r1.size());
+    std::printf("meas_two %zu\n", r2.size());
+    std::printf("meas_center %ld\n", dmps.GetCenter());
+  }
 
   // TruncateMPS to D = 2: every bond at most 2, the state stays normalised
   {

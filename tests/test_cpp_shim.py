@@ -4,7 +4,8 @@ the Python side, ``DirectStateInitMps``, ``SiteVec``, ``TenVec``), and on the
 GPU the reference's 1DHeisenberg DMRG case restated in C++
 (``test_two_site_update_finite_vmps.cc:186-220``: golden energy
 -2.493577133888 to 1e-12, then a resumed call), a ``LanczosSolver``,
-``FiniteMPS::Centralize`` and ``TruncateMPS`` through the same header."""
+``FiniteMPS::Centralize``, ``TruncateMPS`` and the measurements through the
+same header (against the Python API on the same state)."""
 import os
 import subprocess
 
@@ -48,6 +49,10 @@ def test_cpp_shim_host(shim_exe, tmp_path):
     rc, out, err = _run(shim_exe, "host", tmp_path, 60)
     assert rc == 0, out + err
     assert "host ok" in out
+    # DumpMeasuRes writes what the Python DumpMeasuRes writes
+    from mps2_gb300.measure import DumpMeasuRes, MeasuResElem
+    DumpMeasuRes([MeasuResElem([0], 0.25), MeasuResElem([1, 4], -0.125)], str(tmp_path / "py"))
+    assert (tmp_path / "measu.json").read_text() == (tmp_path / "py.json").read_text()
     # the C++ writer reproduces the Python file byte for byte
     assert (tmp_path / "out.gqten").read_bytes() == (tmp_path / "in.gqten").read_bytes()
     # DirectStateInitMps agrees with the Python one
@@ -87,5 +92,27 @@ def test_cpp_shim_dmrg(shim_exe, tmp_path):
     assert int(vals["truncate_bonds"]) == 5
     assert int(vals["truncate_dmax"]) == 2
     assert abs(float(vals["truncate_norm"]) - 1.0) <= 1e-12
+    # measurements through the C++ header against the Python API on the same
+    # MPS (finite_mps_measu.h); the singlet ground state has <Sz_i> = 0
+    import json
+    from mps2_gb300.finite_mps import FiniteMPS
+    from mps2_gb300.measure import MeasureOneSiteOp, MeasureTwoSiteOp
+    sv, _, _, _ = H.heisenberg_chain(6)
+    _, ops = H.spin_half_ops()
+    pm = FiniteMPS(sv)
+    pm.Load(str(tmp_path / "mps_meas"))
+    py1 = MeasureOneSiteOp(pm, ops["sz"], str(tmp_path / "py_sz"))
+    pairs = [[0, 1], [0, 3], [2, 5], [1, 4]]
+    py2 = MeasureTwoSiteOp(pm, [ops["sz"], ops["sz"]], ops["id"], pairs, str(tmp_path / "py_szsz"))
+    c1 = json.load(open(tmp_path / "sz.json"))
+    c2 = json.load(open(tmp_path / "szsz.json"))
+    assert int(vals["meas_one"]) == 6 and int(vals["meas_two"]) == 4
+    assert vals["meas_center"] == "1"   # the last event started at site 1
+    assert [e[0] for e in c1] == [[i] for i in range(6)] and [e[0] for e in c2] == pairs
+    for (sites, v), e in zip(c1, py1):
+        assert abs(v - e.avg) <= 1e-11 and abs(v) <= 1e-10
+    for (sites, v), e in zip(c2, py2):
+        assert abs(v - e.avg) <= 1e-11
+    assert c2[0][1] < -0.1   # nearest neighbours anti-aligned
     # split form: 3xTF32 products, FP64-accurate energy; 1e-9 relative
     assert abs(float(vals["e0_split"]) - GOLDEN_1D_HEISENBERG) <= 1e-9 * abs(GOLDEN_1D_HEISENBERG)
