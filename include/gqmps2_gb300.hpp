@@ -512,13 +512,23 @@ inline void CreatPath(const std::string &path) {
 }
 
 enum MPSTenCanoType { NONE = GQ_CANO_NONE, LEFT = GQ_CANO_LEFT, RIGHT = GQ_CANO_RIGHT };
+const long kUncentralizedCenterIdx = -1;
 
 class FiniteMPS : public TenVec<GQTensor> {
  public:
   explicit FiniteMPS(const SiteVec &sv)
       : TenVec<GQTensor>(sv.size), tens_cano_type_(sv.size, NONE), site_vec_(sv) {}
+  /* write access marks the site non-canonical and the MPS uncentralised, as
+   * the reference's non-const accessor does (finite_mps.h:67-75) */
+  GQTensor &operator[](size_t i) {
+    tens_cano_type_.at(i) = NONE;
+    center_ = kUncentralizedCenterIdx;
+    return TenVec<GQTensor>::operator[](i);
+  }
+  const GQTensor &operator[](size_t i) const { return TenVec<GQTensor>::operator[](i); }
   const SiteVec &GetSitesInfo() const { return site_vec_; }
   std::vector<MPSTenCanoType> GetTensCanoType() const { return tens_cano_type_; }
+  MPSTenCanoType GetTenCanoType(size_t i) const { return tens_cano_type_.at(i); }
   long GetCenter() const { return center_; }
   void Dump(const std::string &mps_path = kMpsPath, bool release_mem = false) {
     CreatPath(mps_path);
@@ -531,13 +541,14 @@ class FiniteMPS : public TenVec<GQTensor> {
    * be loaded; the tensors are replaced by the canonicalised ones. */
   void Centralize(long target_center) {
     const int n = (int)size();
+    std::vector<int> cano(tens_cano_type_.begin(), tens_cano_type_.end());
+    const FiniteMPS &self = *this;  // reads leave the canonical types alone
     std::vector<DeviceTensor> d;
     std::vector<gq_tensor *> h;
     for (int i = 0; i < n; ++i) {
-      d.push_back(DeviceTensor::FromHost((*this)[i]));
+      d.push_back(DeviceTensor::FromHost(self[i]));
       h.push_back(d.back().get());
     }
-    std::vector<int> cano(tens_cano_type_.begin(), tens_cano_type_.end());
     Check(gq_mps_centralize(h.data(), n, (int)target_center, cano.data()));
     for (int i = 0; i < n; ++i) {  // the handles' tensors were rewritten in place
       (*this)[i] = d[i].ToHost();
@@ -546,7 +557,7 @@ class FiniteMPS : public TenVec<GQTensor> {
     center_ = target_center;
   }
   std::vector<MPSTenCanoType> tens_cano_type_;
-  long center_ = -1;
+  long center_ = kUncentralizedCenterIdx;
 
  private:
   SiteVec site_vec_;
@@ -561,13 +572,14 @@ inline void TruncateMPS(FiniteMPS &mps, double trunc_err, size_t Dmin, size_t Dm
                         std::vector<int64_t> *dims = nullptr) {
   const int n = (int)mps.size();
   if (n < 2) throw Error("TruncateMPS: at least two sites");
+  std::vector<int> cano(mps.tens_cano_type_.begin(), mps.tens_cano_type_.end());
+  const FiniteMPS &cm = mps;
   std::vector<DeviceTensor> d;
   std::vector<gq_tensor *> h;
   for (int i = 0; i < n; ++i) {
-    d.push_back(DeviceTensor::FromHost(mps[i]));
+    d.push_back(DeviceTensor::FromHost(cm[i]));
     h.push_back(d.back().get());
   }
-  std::vector<int> cano(mps.tens_cano_type_.begin(), mps.tens_cano_type_.end());
   std::vector<double> e(n - 1);
   std::vector<int64_t> D(n - 1);
   Check(gq_mps_truncate(h.data(), n, cano.data(), trunc_err, (int64_t)Dmin, (int64_t)Dmax,
@@ -740,8 +752,10 @@ inline double FullContract(const GQTensor &a, const GQTensor &b, const std::vect
 /* the MPS on the device with the reference's canonical-type bookkeeping */
 struct DeviceMPS {
   explicit DeviceMPS(FiniteMPS &m) : host(m), n((int)m.size()) {
-    for (int i = 0; i < n; ++i) t.push_back(DeviceTensor::FromHost(m[i]));
     cano.assign(m.tens_cano_type_.begin(), m.tens_cano_type_.end());
+    const FiniteMPS &cm = m;
+    for (int i = 0; i < n; ++i) t.push_back(DeviceTensor::FromHost(cm[i]));
+    center = m.GetCenter();
   }
   void Centralize(int c) {
     std::vector<gq_tensor *> h;

@@ -107,8 +107,15 @@ def read_tensor(path: str) -> GQTensor:
     return t
 
 
+kUncentralizedCenterIdx = -1
+
+
 class FiniteMPS:
-    """A finite MPS: ``N`` optional site tensors plus the site information."""
+    """A finite MPS: ``N`` optional site tensors plus the site information.
+
+    As the reference's non-const accessors do (``finite_mps.h:67-89``),
+    assigning a site tensor marks that site non-canonical and the MPS
+    uncentralised; ``Centralize`` and the initialisers set both afterwards."""
 
     # canonical types of the site tensors (``MPSTenCanoType``)
     NONE, LEFT, RIGHT = 0, 1, 2
@@ -116,14 +123,17 @@ class FiniteMPS:
     def __init__(self, site_vec: SiteVec):
         self.site_vec = site_vec
         self.tens: List[Optional[GQTensor]] = [None] * site_vec.size
-        self.center = None
+        self.center = kUncentralizedCenterIdx
         self.tens_cano_type = [FiniteMPS.NONE] * site_vec.size
 
-    def GetCenter(self):
+    def GetCenter(self) -> int:
         return self.center
 
     def GetTensCanoType(self) -> List[int]:
         return list(self.tens_cano_type)
+
+    def GetTenCanoType(self, i: int) -> int:
+        return self.tens_cano_type[i]
 
     def Centralize(self, target_center: int) -> None:
         """``FiniteMPS::Centralize`` (``finite_mps.h:149-248``) on the GPU:
@@ -146,6 +156,8 @@ class FiniteMPS:
 
     def __setitem__(self, i, t: GQTensor):
         self.tens[i] = t
+        self.tens_cano_type[i] = FiniteMPS.NONE
+        self.center = kUncentralizedCenterIdx
 
     def empty(self) -> bool:
         return all(t is None for t in self.tens)

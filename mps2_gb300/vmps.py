@@ -30,6 +30,7 @@ import numpy as np
 from . import _lib
 from ._lib import DeviceTensor, check, load
 from .finite_mps import (FiniteMPS, GenEnvTenName, GenMPSTenName, kMpsPath, kRuntimeTempPath,
+                         kUncentralizedCenterIdx,
                          read_tensor, write_tensor)
 from .tensor import GQTensor, QN, Div
 
@@ -321,5 +322,5 @@ def TruncateMPS(mps: FiniteMPS, trunc_err: float, Dmin: int, Dmax: int):
     for i, t in enumerate(dev):
         mps[i] = t.to_host()
     mps.tens_cano_type = list(cano)
-    mps.center = None
+    mps.center = kUncentralizedCenterIdx
     return [(float(e), int(d)) for e, d in zip(errs[:n - 1], Ds[:n - 1])]

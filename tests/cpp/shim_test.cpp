@@ -77,6 +77,15 @@ int run_host(const std::string &dir) {
   DirectStateInitMps(mps, labs, QN{0});
   expect(mps.GetTensCanoType()[0] == NONE && mps.GetTensCanoType()[1] == RIGHT,
          "canonical types after DirectStateInitMps");
+  {  // finite_mps.h:67-75: write access marks the site non-canonical, the MPS uncentralised
+    FiniteMPS m2 = mps;
+    const FiniteMPS &c2 = m2;
+    (void)c2[2];
+    expect(m2.GetTenCanoType(2) == RIGHT && m2.GetCenter() == 0, "const access keeps the types");
+    m2[2] = c2[2];
+    expect(m2.GetTenCanoType(2) == NONE && m2.GetCenter() == kUncentralizedCenterIdx,
+           "write access resets the canonical type and the center");
+  }
   mps.Dump(dir + "/mps", true);
   expect(mps.empty(), "Dump with release empties the MPS");
 

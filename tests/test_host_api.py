@@ -113,3 +113,20 @@ def test_ten_vec_io(tmp_path):
     v.LoadTen(2, names[1])
     for got, want in zip((v[0], v[1], v[2]), (tens[2], tens[0], tens[1])):
         assert got.indices == want.indices and got.dense_equal(want)
+
+
+def test_finite_mps_write_access_resets_canonical_types():
+    """``finite_mps.h:67-75``: writing a site marks it non-canonical and the
+    MPS uncentralised; reading does not."""
+    from mps2_gb300 import hamiltonians as H
+    from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS, kUncentralizedCenterIdx
+    sv, _, qn0, _ = H.heisenberg_chain(6)
+    mps = FiniteMPS(sv)
+    assert mps.GetCenter() == kUncentralizedCenterIdx
+    DirectStateInitMps(mps, [i % 2 for i in range(6)], qn0)
+    assert mps.GetCenter() == 0 and mps.GetTenCanoType(3) == FiniteMPS.RIGHT
+    t = mps[3]
+    assert mps.GetTenCanoType(3) == FiniteMPS.RIGHT
+    mps[3] = t
+    assert mps.GetTenCanoType(3) == FiniteMPS.NONE
+    assert mps.GetCenter() == kUncentralizedCenterIdx
