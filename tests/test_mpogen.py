@@ -88,3 +88,61 @@ def test_hubbard_chain_mpo_is_the_hamiltonian():
         h += chain({a: d["nadn"], b: -1.0 * d["fadagdn"]})
     np.testing.assert_allclose(_dense_mpo(mpo), h, atol=1e-12)
     assert max(w.indices[-1].dim for w in mpo[1:-1]) == 6
+
+
+def test_random_terms_mpo_is_the_sum_of_terms():
+    """Seeded random Hamiltonians on 5 sites: one- to three-site operator
+    strings (S^z, S^+, S^-, identity inside), coefficients drawn from a small
+    set so that coefficient labels repeat and the compression moves shared
+    coefficients between matrices.  Only charge-conserving strings are kept.
+    The generated MPO, contracted, equals the sum of the terms."""
+    from mps2_gb300.mpogen import MPOGenerator
+    from mps2_gb300.site_vec import SiteVec
+    pb, ops = H.spin_half_ops()
+    d = {k: to_oracle(v).to_dense() for k, v in ops.items()}
+    charge = {"sz": 0, "sp": 1, "sm": -1, "id": 0}
+    rng = np.random.default_rng(20240)
+    n = 5
+    for trial in range(12):
+        gen = MPOGenerator(SiteVec(n, pb), (0,))
+        h = np.zeros((2 ** n, 2 ** n))
+        coefs = [0.5, -1.25, 2.0, 0.5, 1.0]
+        seen_one_site = set()
+        for _ in range(rng.integers(4, 12)):
+            k = int(rng.integers(1, 4))
+            sites = sorted(rng.choice(n, size=k, replace=False).tolist())
+            names = [str(rng.choice(["sz", "sp", "sm"])) for _ in sites]
+            if sum(charge[x] for x in names) != 0:
+                continue
+            c = float(rng.choice(coefs))
+            gen.AddTerm(c, [ops[x] for x in names], sites)
+            if k == 1:  # the reference keeps one copy of an identical one-site term
+                if (names[0], sites[0], c) in seen_one_site:
+                    continue
+                seen_one_site.add((names[0], sites[0], c))
+            m = np.array([[1.0]])
+            for s in range(n):
+                m = np.kron(m, d[names[sites.index(s)]] if s in sites else np.eye(2))
+            h += c * m
+        if not np.any(h):
+            continue
+        mpo = gen.Gen()
+        np.testing.assert_allclose(_dense_mpo(mpo), h, atol=1e-13, err_msg=f"trial {trial}")
+
+
+def test_identical_one_site_term_counts_once():
+    """The reference's FSM keeps an existing element when the added one is
+    equal to it (``fsm.h:230-239``), so the same one-site term added twice
+    is counted once, while two equal two-site terms add up (their paths
+    run through different middle states)."""
+    from mps2_gb300.mpogen import MPOGenerator
+    from mps2_gb300.site_vec import SiteVec
+    pb, ops = H.spin_half_ops()
+    sz = to_oracle(ops["sz"]).to_dense()
+    gen = MPOGenerator(SiteVec(3, pb), (0,))
+    gen.AddTerm(0.5, [ops["sz"]], [1])
+    gen.AddTerm(0.5, [ops["sz"]], [1])
+    gen.AddTerm(1.0, [ops["sz"], ops["sz"]], [0, 2])
+    gen.AddTerm(1.0, [ops["sz"], ops["sz"]], [0, 2])
+    want = 0.5 * _site_op(sz, 1, 3) + 2.0 * _site_op(sz, 0, 3) @ _site_op(sz, 2, 3)
+    np.testing.assert_allclose(_dense_mpo(gen.Gen()), want, atol=1e-14)
