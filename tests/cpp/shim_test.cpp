@@ -119,6 +119,23 @@ int run_host(const std::string &dir) {
   tv.LoadTen(2, dir + "/ten1.gqten");
   expect(tv[0] == t2 && tv[1] == t0 && tv[2] == t1, "TenVec load after dump");
 
+  // test_mpo.cc:42-67: an MPO of N default tensors; element access
+  {
+    MPO<GQTensor> empty_mpo(0);
+    expect(empty_mpo.size() == 0, "MPO of size 0");
+    MPO<GQTensor> mpo(5);
+    bool all_default = mpo.size() == 5;
+    for (size_t i = 0; i < mpo.size(); ++i) all_default = all_default && mpo[i] == GQTensor();
+    expect(all_default, "MPO elements start as default tensors");
+    MPO<GQTensor> m3(3);
+    m3[0] = t0;
+    m3[1] = t1;
+    m3[2] = t2;
+    expect(m3[0] == t0 && m3[1] == t1 && m3[2] == t2, "MPO element assignment");
+    m3[1] = t2;
+    expect(m3[1] == t2, "MPO element reassignment");
+  }
+
   // test_duovector.cc: copies own their elements, moves take them over
   TenVec<GQTensor> copy(tv);
   expect(copy.size() == 3 && copy[0] == tv[0] && copy(0) != tv(0), "TenVec copy is deep");
