@@ -66,9 +66,10 @@ def _args():
     p.add_argument("--precision", choices=["fp64", "tf32x3", "fp64tc"], default="tf32x3")
     p.add_argument("--rayleigh", choices=["fp64", "fp64tc"], default="fp64tc",
                    help="arithmetic of the split form's Rayleigh-quotient energies")
-    p.add_argument("--model", choices=["heisenberg", "hubbard"], default="heisenberg",
+    p.add_argument("--model", choices=["heisenberg", "hubbard", "j1j2"], default="heisenberg",
                    help="heisenberg: L=100 chain, D 500->2000 (headline); hubbard: L=64 "
-                        "chain, U=8, half filling, D 1000->4000")
+                        "chain, U=8, half filling, D 1000->4000; j1j2: 4x16 open cylinder "
+                        "(snake order), J1=1, J2=0.5, D 2000->6000")
     p.add_argument("--schedule", default=None,
                    help="comma-separated D per growth sweep; the last is the timed D")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -170,15 +171,22 @@ def _fp64_peak_tflops(torch):
 
 HUBBARD = {"L": 64, "schedule": [1000, 1430, 1860, 2290, 2710, 3140, 3570, 4000],
            "workload": "hubbard_obc_L64_U8_half_filling_D1000to4000"}
+J1J2 = {"L": 64, "Lx": 16, "Ly": 4, "J1": 1.0, "J2": 0.5,
+        "schedule": [2000, 2570, 3140, 3710, 4290, 4860, 5430, 6000],
+        "workload": "j1j2_cylinder_4x16_snake_J2_0.5_D2000to6000"}
 
 
 def _select_model(args):
     """Module constants for the chosen model (heisenberg: the headline chain;
     hubbard: L=64, t=1, U=8, half filling, Sz=0, U(1)xU(1), Jordan-Wigner
-    MPO of bond dimension 6, alternating up/down product state)."""
+    MPO of bond dimension 6, alternating up/down product state; j1j2: the
+    4x16 open cylinder in snake order, J1=1, J2=0.5, Sz=0, shuffled Neel
+    product state, MPO from the generator's compression, bond dimension <= 17)."""
     global L_SITES, WORKLOAD, SCHEDULE
     if args.model == "hubbard":
         L_SITES, WORKLOAD, SCHEDULE = HUBBARD["L"], HUBBARD["workload"], HUBBARD["schedule"]
+    elif args.model == "j1j2":
+        L_SITES, WORKLOAD, SCHEDULE = J1J2["L"], J1J2["workload"], J1J2["schedule"]
     if args.schedule is None:
         args.schedule = ",".join(map(str, SCHEDULE))
 
@@ -189,6 +197,10 @@ def _model(model="heisenberg"):
     if model == "hubbard":
         sv, mpo, qn0, gen = H.hubbard_chain(L_SITES, 1.0, 8.0)
         labels = [1 if i % 2 == 0 else 2 for i in range(L_SITES)]
+    elif model == "j1j2":
+        pairs = H.j1j2_cylinder_pairs(J1J2["Lx"], J1J2["Ly"], J1J2["J1"], J1J2["J2"])
+        sv, mpo, qn0, gen = H.heisenberg_pairs(L_SITES, pairs)
+        labels = H.neel_shuffled_labels(L_SITES, 0)
     else:
         sv, mpo, qn0, gen = H.heisenberg_chain(L_SITES)
         labels = H.neel_shuffled_labels(L_SITES, 0)

@@ -130,3 +130,26 @@ def test_finite_mps_write_access_resets_canonical_types():
     mps[3] = t
     assert mps.GetTenCanoType(3) == FiniteMPS.NONE
     assert mps.GetCenter() == kUncentralizedCenterIdx
+
+
+def test_j1j2_cylinder_workload_definition():
+    """The J1-J2 4x16 cylinder workload: 64 sites, D 2000 -> 6000 over eight
+    calls, an Sz = 0 product state, the generator's MPO (bulk bond dimension
+    at most 17 after compression)."""
+    import argparse
+    import bench
+    args = argparse.Namespace(model="j1j2", schedule=None)
+    saved = (bench.L_SITES, bench.WORKLOAD, bench.SCHEDULE)
+    try:
+        bench._select_model(args)
+        assert bench.L_SITES == 64 and args.schedule.split(",")[0] == "2000"
+        assert args.schedule.split(",")[-1] == "6000" and len(args.schedule.split(",")) == 8
+        mps, mpo = bench._model("j1j2")
+        assert mps.size() == 64 and len(mpo) == 64
+        assert max(w.indices[-1].dim for w in mpo[1:-1]) <= 17
+        # total Sz = 0: the head tensor's right bond carries the charge of sites 1..N-1
+        # and the head site's own charge cancels it
+        q_head = tuple(mps[0].div)
+        assert q_head == (0,)
+    finally:
+        bench.L_SITES, bench.WORKLOAD, bench.SCHEDULE = saved
