@@ -179,8 +179,10 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
   check_device_errors();
   st.update_seconds = seconds_since(t0);
   if (prm.verbose) {
-    std::printf("Site %4d E0 = %20.16f TruncErr = %.2e D = %5lld Iter = %3lld LanczT = %8.3f "
-                "TotT = %8.3f S = %10.7f\n",
+    // the reference's stream state: fixed, precision 16 for E0, 2 after the
+    // scientific TruncErr, 7 for S
+    std::printf("Site %4d E0 = %20.16f TruncErr = %.2e D = %5lld Iter = %3lld LanczT = %8.2f "
+                "TotT = %8.2f S = %10.7f\n",
                 target, st.e0, st.trunc_err, (long long)st.D, (long long)st.iters,
                 st.lanczos_seconds, st.update_seconds, st.ee);
     std::fflush(stdout);

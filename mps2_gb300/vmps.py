@@ -81,8 +81,8 @@ class UpdateStats:
     def line(self) -> str:
         """The reference's per-update log line (``:329-338``)."""
         return (f"Site {self.site:4d} E0 = {self.e0:20.16f} TruncErr = {self.trunc_err:.2e} "
-                f"D = {self.D:5d} Iter = {self.iters:3d} LanczT = {self.lanczos_seconds:8.3f} "
-                f"TotT = {self.update_seconds:8.3f} S = {self.ee:10.7f}")
+                f"D = {self.D:5d} Iter = {self.iters:3d} LanczT = {self.lanczos_seconds:8.2f} "
+                f"TotT = {self.update_seconds:8.2f} S = {self.ee:10.7f}")
 
 
 def run_batch(states: Sequence["DMRGState"], params: Sequence[SweepParams],

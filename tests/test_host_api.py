@@ -153,3 +153,17 @@ def test_j1j2_cylinder_workload_definition():
         assert q_head == (0,)
     finally:
         bench.L_SITES, bench.WORKLOAD, bench.SCHEDULE = saved
+
+
+def test_update_log_line_format():
+    """The per-update line of ``two_site_update_finite_vmps_impl.h:330-338``:
+    fixed notation, E0 with 16 decimals, TruncErr in scientific with 2, the
+    two timings with 2, S with 7."""
+    from mps2_gb300 import _lib
+    from mps2_gb300.vmps import UpdateStats
+    c = _lib.UpdateStatsC()
+    c.site, c.dir, c.e0, c.trunc_err, c.D, c.iters = 7, ord("r"), -2.4935771338879276, 1.25e-9, 8, 12
+    c.ee, c.lanczos_seconds, c.update_seconds = 0.6931471805599453, 0.0123, 1.5
+    line = UpdateStats(c).line()
+    assert line == ("Site    7 E0 =  -2.4935771338879276 TruncErr = 1.25e-09 D =     8 Iter =  12 "
+                    "LanczT =     0.01 TotT =     1.50 S =  0.6931472")
