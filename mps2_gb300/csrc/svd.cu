@@ -660,8 +660,18 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     const int nslot = (int)std::min<size_t>(solves.size(), 1 + Lane::kAux);
     for (size_t k = 0; k < solves.size(); ++k) solves[k].slot = (int)(k % nslot);
     auto handle_of = [&](int slot) { return slot == 0 ? h : aux_solver(slot - 1); };
-    std::vector<cusolverDnParams_t> sp(nslot);
-    for (auto &x : sp) GQ_SOLVER(cusolverDnCreateParams(&x));
+    struct ParamsSet {  // released on every exit path
+      std::vector<cusolverDnParams_t> v;
+      ~ParamsSet() {
+        for (auto x : v) cusolverDnDestroyParams(x);
+      }
+    } params;
+    for (int k = 0; k < nslot; ++k) {
+      cusolverDnParams_t x = nullptr;
+      GQ_SOLVER(cusolverDnCreateParams(&x));
+      params.v.push_back(x);
+    }
+    const std::vector<cusolverDnParams_t> &sp = params.v;
     std::vector<size_t> dws(nslot, 0), hws(nslot, 0);
     for (const Solve &v : solves) {
       size_t d1 = 0, h1 = 0;
@@ -693,7 +703,6 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
             CUDA_R_64F, dwork[v.slot].p, dws[v.slot], hwork[v.slot].data(), hws[v.slot],
             einfo.p + v.io, v.nb));
     }
-    for (auto &x : sp) cusolverDnDestroyParams(x);
   }
   prof_end(kProfSvdEig, 0.0, 0.0);
   // ---- values to the host ---------------------------------------------------
