@@ -151,12 +151,16 @@ int gq_contract(const gq_tensor *a, const gq_tensor *b, int naxes, const int *ax
  * with GQ_PREC_FP64, written into `out`, which the caller creates beforehand
  * (gq_tensor_create) with a's free legs then b's free legs, divergence
  * div(a) + div(b), and every block the contraction produces.  Scratch lives
- * in arrays the library reserves on each GPU when it is loaded (about
- * 22 MiB, kept until exit): a and b together may hold at most 2^21
+ * in file-scope device arrays (about 22 MiB on each GPU that uses the
+ * library, kept until exit): a and b together may hold at most 2^21
  * elements, with at most 2^15 output tiles of 64 x 64, 2^17 block products
- * and 2^15 permute tasks; larger inputs return GQ_ERR_INVALID.  The first
- * call on a device looks the arrays up (do it before any stream capture).
- * Calls share the arrays: calls that overlap on the GPU race. */
+ * and 2^15 permute tasks; larger inputs return GQ_ERR_INVALID.  gq_init
+ * looks the arrays up and loads this entry point's kernels on its device
+ * (CUDA loads modules lazily, and that load may allocate); without gq_init,
+ * the first call on a device does it, so make that first call before the
+ * no-allocation phase and before any stream capture.  Each call returns
+ * after its GPU work has finished.  Calls share the arrays: calls that
+ * overlap on the GPU race. */
 int gq_contract_noalloc(const gq_tensor *a, const gq_tensor *b, int naxes, const int *axes_a,
                         const int *axes_b, gq_tensor *out);
 

@@ -277,6 +277,9 @@ void check_device_errors();
 // allocation (noalloc.cu).
 void contract_noalloc(const Tensor &a, const Tensor &b, const std::vector<int> &axes_a,
                       const std::vector<int> &axes_b, Tensor &out);
+// Its once-per-device set-up (array addresses, lazy module load), run by
+// init_context for the context's device.
+void noalloc_setup();
 
 // ---------------------------------------------------------------------------
 // Vector kernels (vecops.cu).  Scalars live in device memory so the Lanczos

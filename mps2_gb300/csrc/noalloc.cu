@@ -15,16 +15,22 @@
 // How: the two operands are permuted into matrix form inside a file-scope
 // device array (g_na_operands, kNaOperandElems doubles = 16 MiB) and the
 // per-call work lists go to three more file-scope arrays (about 6 MiB in
-// all).  Every GPU that loads the library keeps these ~22 MiB until the
+// all).  Every GPU that uses the library keeps these ~22 MiB until the
 // process exits.  Host code cannot use the arrays' names as device
-// addresses, so on the first call on each device (with that device
-// current) the entry point looks their addresses up once with
-// cudaGetSymbolAddress and passes them to the kernels; make that first call
-// before any stream capture.  All calls share the arrays and each call
+// addresses, so a set-up step, once per device and with that device
+// current, looks their addresses up with cudaGetSymbolAddress and launches
+// each kernel of this file once with no work.  CUDA loads a module's
+// device memory and kernels lazily (CUDA_MODULE_LOADING=LAZY is the default
+// since CUDA 12.2), and that load can allocate and synchronise; the set-up
+// makes it happen there.  gq_init runs the set-up for its device; a caller
+// that skips gq_init gets it inside its first call of this entry point on
+// that device, and must make that first call before its no-allocation phase
+// and before any stream capture.  All calls share the arrays and each call
 // rewrites every element it later reads, so nothing needs clearing between
-// calls; two calls whose work overlaps on the GPU (different streams,
-// threads or devices sharing a context) race on the arrays and must not be
-// issued concurrently.
+// calls; two calls whose work overlaps on the GPU race on the arrays and
+// must not be issued concurrently.  Each call waits for its own GPU work to
+// finish before it returns (the work lists are copied from host memory that
+// the call owns).
 #include <map>
 #include <mutex>
 
@@ -61,6 +67,12 @@ struct NaAddrs {
 std::mutex g_na_mu;
 std::map<int, NaAddrs> g_na_addrs;  // per device
 
+__global__ void na_permute_kernel(const NaPerm *__restrict__ tasks, int ntasks,
+                                  const double *__restrict__ src, double *__restrict__ dst);
+__global__ void na_gemm_kernel(const NaTile *__restrict__ tiles, int ntiles,
+                               const NaPair *__restrict__ pairs, const double *__restrict__ A,
+                               const double *__restrict__ B, double *__restrict__ C);
+
 // Set-up, once per device, with that device current.
 NaAddrs na_addresses() {
   int dev = 0;
@@ -73,12 +85,19 @@ NaAddrs na_addresses() {
   GQ_CUDA(cudaGetSymbolAddress((void **)&a.tiles, g_na_tiles));
   GQ_CUDA(cudaGetSymbolAddress((void **)&a.pairs, g_na_pairs));
   GQ_CUDA(cudaGetSymbolAddress((void **)&a.perm, g_na_perm));
+  // one launch of each kernel with no work, so that lazy module loading
+  // happens here and not inside a later call
+  na_permute_kernel<<<1, 32, 0, stream()>>>(a.perm, 0, nullptr, nullptr);
+  na_gemm_kernel<<<1, 256, 0, stream()>>>(a.tiles, 0, a.pairs, nullptr, nullptr, nullptr);
+  GQ_CUDA(cudaGetLastError());
+  GQ_CUDA(cudaStreamSynchronize(stream()));
   g_na_addrs[dev] = a;
   return a;
 }
 
-__global__ void na_permute_kernel(const NaPerm *__restrict__ tasks, const double *__restrict__ src,
-                                  double *__restrict__ dst) {
+__global__ void na_permute_kernel(const NaPerm *__restrict__ tasks, int ntasks,
+                                  const double *__restrict__ src, double *__restrict__ dst) {
+  if ((int)blockIdx.x >= ntasks) return;  // ntasks == 0: the set-up's empty launch
   __shared__ NaPerm t;
   if (threadIdx.x == 0) t = tasks[blockIdx.x];
   __syncthreads();
@@ -97,9 +116,10 @@ __global__ void na_permute_kernel(const NaPerm *__restrict__ tasks, const double
 // B' row-major k x n (the same 64x64 tiling and summation order as the
 // allocating path's FP64 kernel).
 __global__ void __launch_bounds__(256)
-    na_gemm_kernel(const NaTile *__restrict__ tiles, const NaPair *__restrict__ pairs,
+    na_gemm_kernel(const NaTile *__restrict__ tiles, int ntiles, const NaPair *__restrict__ pairs,
                    const double *__restrict__ A, const double *__restrict__ B,
                    double *__restrict__ C) {
+  if ((int)blockIdx.x >= ntiles) return;  // ntiles == 0: the set-up's empty launch
   constexpr int BM = 64, BN = 64, BK = 16;
   __shared__ double As[BK][BM];
   __shared__ double Bs[BK][BN];
@@ -183,6 +203,8 @@ void na_perm_tasks(const Tensor &t, const std::vector<int> &perm, int64_t base,
 }
 
 }  // namespace
+
+void noalloc_setup() { (void)na_addresses(); }
 
 void contract_noalloc(const Tensor &A, const Tensor &B, const std::vector<int> &xa,
                       const std::vector<int> &xb, Tensor &O) {
@@ -284,14 +306,17 @@ void contract_noalloc(const Tensor &A, const Tensor &B, const std::vector<int> &
     GQ_CUDA(cudaMemcpyAsync(ad.tiles, tiles.data(), sizeof(NaTile) * tiles.size(),
                             cudaMemcpyHostToDevice, s));
   if (na_tasks > 0)
-    na_permute_kernel<<<(unsigned)na_tasks, 256, 0, s>>>(ad.perm, A.data.p, ad.operands);
-  if (perm.size() > na_tasks)
-    na_permute_kernel<<<(unsigned)(perm.size() - na_tasks), 256, 0, s>>>(ad.perm + na_tasks,
-                                                                         B.data.p, ad.operands);
+    na_permute_kernel<<<(unsigned)na_tasks, 256, 0, s>>>(ad.perm, (int)na_tasks, A.data.p,
+                                                         ad.operands);
+  if (perm.size() > na_tasks) {
+    const int nb_tasks = (int)(perm.size() - na_tasks);
+    na_permute_kernel<<<(unsigned)nb_tasks, 256, 0, s>>>(ad.perm + na_tasks, nb_tasks, B.data.p,
+                                                         ad.operands);
+  }
   GQ_CUDA(cudaGetLastError());
   if (!tiles.empty())
-    na_gemm_kernel<<<(unsigned)tiles.size(), 256, 0, s>>>(ad.tiles, ad.pairs, ad.operands,
-                                                           ad.operands, O.data.p);
+    na_gemm_kernel<<<(unsigned)tiles.size(), 256, 0, s>>>(ad.tiles, (int)tiles.size(), ad.pairs,
+                                                           ad.operands, ad.operands, O.data.p);
   GQ_CUDA(cudaGetLastError());
   // the host work lists above are copied from pageable memory; finish
   // before they go out of scope and before the caller reads the output

@@ -44,6 +44,7 @@ void init_context(int device) {
   GQ_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
   init_lane(c->main);
   g_ctx = c;
+  noalloc_setup();
 }
 
 namespace {

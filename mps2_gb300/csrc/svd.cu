@@ -502,8 +502,14 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   prof_begin(kProfSvdEig);
   auto h = solver();
   auto bh = blas();
-  gesvdjInfo_t prm;
-  GQ_SOLVER(cusolverDnCreateGesvdjInfo(&prm));
+  struct JacobiInfo {  // released on every exit path
+    gesvdjInfo_t p = nullptr;
+    ~JacobiInfo() {
+      if (p) cusolverDnDestroyGesvdjInfo(p);
+    }
+  } jinfo_guard;
+  GQ_SOLVER(cusolverDnCreateGesvdjInfo(&jinfo_guard.p));
+  gesvdjInfo_t prm = jinfo_guard.p;
   // small groups: one batched Jacobi SVD on zero-padded 32 x 32 slots of X
   const int64_t slot = kSmall * kSmall;
   DevBuf sbatch(n_small * slot), su(n_small * slot), sv(n_small * slot), ss(n_small * kSmall);
@@ -726,7 +732,6 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
                             cudaMemcpyDeviceToHost, s));
   }
   sync();
-  cusolverDnDestroyGesvdjInfo(prm);
   for (int v : hinfo_s)
     if (v != 0) fail(kSolverError, "batched gesvdj did not converge, info=" + std::to_string(v));
   for (int v : hinfo_j)

@@ -79,3 +79,42 @@ def test_noalloc_rejects_oversized_operands():
                                  xb.ctypes.data_as(_lib._IP), do.h)
     assert rc == 1
     assert b"no-allocation scratch" in lib.gq_last_error()
+
+
+def test_noalloc_large_blocks_and_unreached_block_against_oracle():
+    """Sector dimensions of 60 to 150, so that output blocks span several 64 x 64
+    tiles and operand blocks exceed one 16384-element permute chunk; the
+    contracted leg comes first in a, so a is permuted; the caller's output
+    holds every block its legs allow, some of which no block pair reaches:
+    those must come back as exact zeros.  Checked against the FP64 oracle
+    and against gq_contract, on two calls in a row."""
+    import oracle
+    from _convert import to_oracle
+    from mps2_gb300 import _lib
+    from mps2_gb300.tensor import Index
+    from mps2_gb300.vmps import Contract
+    lib = _lib.load()
+    _lib.check(lib.gq_init(0))
+    rng = np.random.default_rng(2024)
+    c = Index([((-1,), 90), ((0,), 120), ((1,), 140)], IN)
+    l0 = Index([((-1,), 110), ((0,), 130), ((1,), 75)], OUT)
+    l1 = Index([((0,), 2), ((1,), 2)], OUT)
+    e = Index([((-1,), 80), ((0,), 100), ((2,), 60)], IN)
+    a = random_tensor(rng, [c, l0, l1], (0,), fill=1.0)
+    b = random_tensor(rng, [c.inverse(), e], (0,), fill=1.0)
+    assert a.size() + b.size() < 2 ** 21
+    assert max(v.size for v in a.blocks.values()) > 16384
+    ref = oracle.contract(to_oracle(a), to_oracle(b), [0], [0])
+    reg = Contract(a, b, ([0], [0]), precision="fp64")
+    full = GQTensor([l0, l1, e], (0,))
+    unreached = [k for k in full.allowed_coords((0,)) if k not in ref.blocks]
+    assert unreached, "the case must hold an output block that no pair reaches"
+    out = GQTensor(full.indices, full.div,
+                   {k: np.full(full.block_shape(k), 1e300) for k in full.allowed_coords((0,))})
+    assert any(v.shape[0] * v.shape[1] > 64 and v.shape[2] > 64 for v in ref.blocks.values())
+    for call in range(2):
+        got = _contract_noalloc(lib, a, b, ([0], [0]), out)
+        for k in unreached:
+            assert np.all(got.blocks[k] == 0.0), (k, call)
+        assert rel_err(got, ref) <= TOL, call
+        assert rel_err(got, reg) <= TOL, call
