@@ -257,7 +257,10 @@ int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *para
 #define GQ_PROF_SVD_EIG 7 /* its decompositions */
 #define GQ_PROF_SVD_GATHER 8  /* its gather of the groups */
 #define GQ_PROF_SVD_FACTORS 9 /* its factor assembly */
-#define GQ_PROF_SVD_ORTHO 10  /* of which CholeskyQR2 */
+#define GQ_PROF_SVD_ORTHO 10  /* of which the QR of null-space completions */
+#define GQ_PROF_SVD_GRAM 11   /* of the decompositions: the Gram matrices */
+#define GQ_PROF_SVD_REDUCE 12 /* of the decompositions: their rank-revealing
+                                 reduction, rank read-back included */
 int gq_profile_enable(int on);
 /* Tile-choice autotuner (not in the reference): with `on`, every matvec
  * contraction whose block-size histogram has not been seen before times the

@@ -81,8 +81,10 @@ enum ProfKernel : int {
   kProfSvdEig = 7,     // its decompositions (cuSOLVER eigensolves / Jacobi, Gram GEMMs)
   kProfSvdGather = 8,  // its gather of the groups into dense matrices
   kProfSvdFactors = 9, // its factor assembly (copies, projections, sign fix, completion)
-  kProfSvdOrtho = 10,  // of which: CholeskyQR2 of transposed-route factors
-  kProfCount = 11,
+  kProfSvdOrtho = 10,  // of which: QR of the null-space completions
+  kProfSvdGram = 11,   // of the decompositions: the Gram matrices
+  kProfSvdReduce = 12, // of the decompositions: rank-revealing reduction and rank read-back
+  kProfCount = 13,
 };
 bool prof_on();
 void prof_enable(bool on);
@@ -249,6 +251,7 @@ void cache_operand(ContractPlan &p, int which, const double *src);
 // Tall-skinny kernel (launched by run_contract when use_skinny).
 bool skinny_eligible_sizes(int64_t a_elems, int64_t b_elems);
 bool skinny_eligible(const Tensor &b, int64_t max_k, int64_t max_n);
+int skinny_max_free_legs();  // free legs of A the kernel handles
 void launch_skinny(const ContractPlan &p, const double *A, const double *B, double *C);
 int skinny_rows_per_cta();
 
@@ -263,6 +266,7 @@ void run_oz_pack(const OzPackPlan &pp, const double *src, const OzPacked &dst);
 void launch_gemm_fp64tc(const ContractPlan &p, const OzPacked &A, const OzPacked &B, double *C);
 int oz_tile_m();
 int oz_tile_n();
+int64_t oz_max_k();  // k of one FP64-accurate output tile, summed over its pairs
 void build_tc_pack(const Tensor &t, const std::vector<int> &row_legs,
                    const std::vector<int> &k_legs, TcPackPlan &pp);
 void run_tc_pack(const TcPackPlan &pp, const double *src, float *dst);
@@ -317,6 +321,25 @@ struct SvdOut {
 // scale_side: 0 none, 1 multiply U columns by s (U.S), 2 multiply Vt rows (S.Vt)
 SvdOut svd_truncate(const Tensor &t, int ldims, const QN &ldiv, double trunc_err,
                     int64_t dmin, int64_t dmax, int scale_side);
+
+// Rank-revealing reduction of Gram matrices (pcmgs.cu): pivoted Cholesky
+// of G (n x n at g_off) with Gram-Schmidt re-orthogonalised columns,
+// G ~ Q T T^T Q^T, stopped when the largest remaining diagonal entry is at
+// most tol times G's largest diagonal entry or after rcap columns.  Writes
+// L and Q (n x rcap, row-major, at q_off), T and C = T T^T (rcap x rcap,
+// row-major, at t_off) and the rank r (-1 when rcap columns did not reach
+// the tolerance).  groups_small (at most 512 rows) run on 4-CTA clusters,
+// groups_big (up to pcmgs_max_rows() rows) on 16-CTA clusters, or 8-CTA
+// ones where the device cannot schedule 16.
+struct PcGroup {
+  int64_t g_off, q_off, t_off;
+  int n, rcap;
+};
+int pcmgs_max_rows();
+int pcmgs_max_rank();
+void launch_pcmgs(const PcGroup *groups_small, int n_small, const PcGroup *groups_big, int n_big,
+                  const double *G, double *L, double *Q, double *T, double *C, int *r_small,
+                  int *r_big, double tol);
 
 // ---------------------------------------------------------------------------
 // Tridiagonal eigensolver (tridiag.cpp)

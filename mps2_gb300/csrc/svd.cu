@@ -15,30 +15,31 @@
 //    sum_{i>=D} s_i^2 / sum s^2 <= trunc_err, capped by Dmax and #values;
 //  * kept nonzero values: the largest-|.| entry of each left vector is made
 //    positive (the right vector follows); kept zero values use the
-//    canonical completion of null_completion (a counter-hashed seed matrix
-//    projected off the group's nonzero singular vectors, then CholeskyQR2)
-//    -- except on a Gram route that solved the canonical side, where the
-//    eigenvectors of the zero eigenvalues serve (see below);
+//    canonical completion of null_completion (the unit vectors the group's
+//    nonzero singular vectors leave, carried through the Householder
+//    reflectors of their QR) -- except on a Gram group solved in full,
+//    where the eigenvectors of the below-floor eigenvalues serve (see
+//    below);
 //  * new bond sectors: groups with a kept value, ascending charge.
 //
 // Decomposition routes (all FP64):
 //  * groups with m, n <= 32: one batched Jacobi SVD for all of them;
 //  * larger groups inside a sweep update: only the factor that becomes the
 //    canonical MPS tensor has to be orthonormal, so it is taken from the
-//    eigenvectors of the Gram matrix on that side (syevd) and the other
-//    factor comes by projection without dividing by singular values --
-//    'r' updates: U from Theta Theta^T and S.Vt = U^T Theta; 'l' updates:
-//    V from Theta^T Theta and U.S = Theta V.  When the other side is much
-//    smaller (at most 0.7x, canonical side >= 256), the eigensolve runs on
-//    the other side's Gram matrix instead and the canonical factor is the
-//    projection through it, column-normalised and orthonormalised by
-//    CholeskyQR2 ('r': U = qr(Theta V), 'l': V = qr(Theta^T U)); the
-//    eigensolve, not the projections, dominates at these sizes.  The Gram
-//    matrices are solved in size buckets with one batched eigensolve per
-//    bucket.  On these
-//    groups eigenvalues below 1e-14 of the group's largest are the
-//    eigensolver's noise floor and count as exact zeros (singular values
-//    below ~1e-7 of the group's largest);
+//    eigenvectors of the Gram matrix on that side and the other factor comes
+//    by projection without dividing by singular values -- 'r' updates: U
+//    from Theta Theta^T and S.Vt = U^T Theta; 'l' updates: V from
+//    Theta^T Theta and U.S = Theta V.  The Gram matrix first goes through a
+//    rank-revealing reduction (pivoted Cholesky with Gram-Schmidt
+//    re-orthogonalised columns, pcmgs.cu): a converged state's Gram matrices
+//    have a numerical rank far below their dimension, and their eigenpairs
+//    above the floor are those of the small matrix T T^T in the basis Q.  A
+//    group whose rank exceeds its cap (about 0.3 of the Gram dimension)
+//    solves its full Gram matrix instead.  The eigensolves run in size
+//    buckets with one batched call per bucket.  On these groups eigenvalues
+//    below 1e-14 of the group's largest are the noise floor of the Gram
+//    matrix and count as exact zeros (singular values below ~1e-7 of the
+//    group's largest);
 //  * larger groups of a plain SVD (both factors orthonormal): Jacobi SVD.
 #include <cublas_v2.h>
 #include <cusolverDn.h>
@@ -54,6 +55,12 @@ namespace {
 constexpr double kZeroSvRtol = 1e-13;
 constexpr double kGramZeroRtol = 1e-14;
 constexpr int kSmall = 32;
+// Rank-revealing reduction of the Gram matrices: stop when the largest
+// remaining diagonal entry is 1e-15 of the largest diagonal entry (a decade
+// below the eigenvalue floor kGramZeroRtol); Gram matrices of at most 512
+// rows run on 4-CTA clusters, larger ones on 16-CTA clusters.
+constexpr double kPcTol = 1e-15;
+constexpr int64_t kPcSmallRows = 512;
 
 enum Route { kSmallJacobi = 0, kJacobi = 1, kGramLeft = 2, kGramRight = 3 };
 
@@ -149,6 +156,20 @@ __global__ void pad_diag_kernel(const PadDiagItem *__restrict__ items, double *_
   }
 }
 
+// A symmetric n x n matrix (leading dimension ld_src) into the top-left of
+// an eigensolve slot (leading dimension ld_dst).
+struct SlotItem { int64_t src_off, dst_off; int n, ld_src, ld_dst; };
+
+__global__ void slot_copy_kernel(const SlotItem *__restrict__ items, const double *__restrict__ src,
+                                 double *__restrict__ dst) {
+  const SlotItem it = items[blockIdx.x];
+  const int64_t nn = (int64_t)it.n * it.n;
+  for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int64_t r = e % it.n, c = e / it.n;
+    dst[it.dst_off + r + c * it.ld_dst] = src[it.src_off + r + c * it.ld_src];
+  }
+}
+
 // Column copies: dst[:, dcol] = src[:, scol] * scale over `rows` rows.
 struct ColItem { int64_t src_off, dst_off; int rows, ld_src, ld_dst, scol, dcol; double scale; };
 
@@ -217,24 +238,14 @@ __global__ void scatter_kernel(const ScatterItem *__restrict__ items, const doub
   }
 }
 
-// Counter-based seed matrix for the null-space completion: element (i, j) =
-// splitmix64(key ^ (i << 20) ^ j), top 53 bits scaled by 2^-53, minus 0.5.
-// Every operation is exact, so the CPU oracle reproduces it bit for bit.
-__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
-  unsigned long long z = x + 0x9E3779B97F4A7C15ull;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
-__global__ void seed_matrix_kernel(double *__restrict__ w, int dim, int k,
-                                   unsigned long long key) {
+// Shifted identity: w (dim x k, col-major) = columns r .. r+k-1 of the
+// dim x dim identity (the unit vectors the completion starts from).
+__global__ void shifted_identity_kernel(double *__restrict__ w, int dim, int k, int r) {
   const int64_t n = (int64_t)dim * k;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long i = (unsigned long long)(e % dim), j = (unsigned long long)(e / dim);
-    const unsigned long long z = splitmix64(key ^ (i << 20) ^ j);
-    w[e] = (double)(z >> 11) * 0x1p-53 - 0.5;
+    const int64_t i = e % dim, j = e / dim;
+    w[e] = (i == r + j) ? 1.0 : 0.0;
   }
 }
 
@@ -245,31 +256,6 @@ void launch_items(void (*kern)(const T *, const double *, double *), const std::
   DevArray<T> d;
   d.upload(items);
   kern<<<(unsigned)items.size(), 256, 0, stream()>>>(d.p, src, dst);
-  GQ_CUDA(cudaGetLastError());
-}
-
-// Column normalisation: each of the k columns (dim entries, ld dim) scaled
-// to unit 2-norm (zero columns stay zero).  One CTA per column.
-__global__ void normalise_columns_kernel(double *__restrict__ q, int dim) {
-  double *c = q + (int64_t)blockIdx.x * dim;
-  __shared__ double part[256];
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < dim; i += blockDim.x) acc = fma(c[i], c[i], acc);
-  part[threadIdx.x] = acc;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) part[threadIdx.x] += part[threadIdx.x + s];
-    __syncthreads();
-  }
-  const double nrm2 = part[0];
-  if (nrm2 <= 0.0) return;
-  const double inv = 1.0 / sqrt(nrm2);
-  for (int i = threadIdx.x; i < dim; i += blockDim.x) c[i] *= inv;
-}
-
-void normalise_columns(double *q, int64_t dim, int64_t k) {
-  if (k == 0) return;
-  normalise_columns_kernel<<<(unsigned)k, 256, 0, stream()>>>(q, (int)dim);
   GQ_CUDA(cudaGetLastError());
 }
 
@@ -307,74 +293,38 @@ void dense_contract_tc(const double *A, int64_t a0, int64_t a1, int axa, const d
                           stream()));
 }
 
-// CholeskyQR2: the k columns of q (dim x k, ld dim) replaced by an
-// orthonormal basis of their span (q <- q R^-1 twice, R from the Cholesky
-// factor of q^T q).
-void cholqr2(double *q, int64_t dim, int64_t k) {
-  if (k == 0) return;
-  auto s = stream();
-  auto bh = blas();
-  auto sh = solver();
-  const int d = (int)dim, kk = (int)k;
-  const double one = 1.0, zero = 0.0;
-  DevBuf g(k * k);
-  int lw = 0;
-  GQ_SOLVER(cusolverDnDpotrf_bufferSize(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, &lw));
-  DevBuf work((int64_t)lw + 1);
-  DevArray<int> info;
-  info.upload(std::vector<int>(2, 0));
-  const bool tc = 2.0 * (double)k * (double)k * (double)dim >= kTcMinFlops;
-  for (int pass = 0; pass < 2; ++pass) {
-    if (tc)  // q col-major d x k = row-major k x d: G = q^T q = Qrow Qrow^T
-      dense_contract_tc(q, k, dim, 1, q, k, dim, 1, g.p);
-    else
-      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, kk, kk, d, &one, q, d, q, d, &zero, g.p,
-                          kk));
-    GQ_SOLVER(cusolverDnDpotrf(sh, CUBLAS_FILL_MODE_LOWER, kk, g.p, kk, work.p, lw,
-                               info.p + pass));
-    GQ_BLAS(cublasDtrsm(bh, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                        CUBLAS_DIAG_NON_UNIT, d, kk, &one, g.p, kk, q, d));
-  }
-  int hinfo[2] = {0, 0};
-  GQ_CUDA(cudaMemcpyAsync(hinfo, info.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
-  sync();
-  if (hinfo[0] != 0 || hinfo[1] != 0) fail(kSolverError, "CholeskyQR2: Cholesky failed");
-}
-
-// Transposed Gram route for a group whose canonical side has `canon` rows
-// and whose other side has `other`: worth it when the other side is much
-// smaller (eigensolve time grows about as n^1.4 at these sizes on GB300,
-// the extra projection and CholeskyQR2 cost a few GEMMs).
-bool transposed_gram(int64_t canon, int64_t other) {
-  return canon >= 256 && (double)other <= 0.7 * (double)canon;
-}
-
 // Canonical completion: k orthonormal columns orthogonal to the r
 // orthonormal columns of `vecs` (dim x r, col-major, ld dim), written to
-// out (dim x k, col-major, ld dim).  The seed matrix is projected off `vecs`
-// twice (Gram-Schmidt with re-orthogonalisation) and orthonormalised by
-// CholeskyQR2; nothing depends on the signs of the columns of `vecs`.
-void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, int group, int side,
-                     double *out) {
+// out (dim x k, col-major, ld dim): columns r .. r+k-1 of the orthogonal
+// factor of the complete Householder QR of `vecs` -- the unit vectors
+// e_r .. e_{r+k-1} carried through its r reflectors (geqrf, then ormqr on
+// the shifted identity; LAPACK's reflector conventions, as the oracle's
+// numpy QR).  O(dim r (r + k)) work, exactly orthonormal whatever the
+// overlap of the unit vectors with `vecs`.  The status words of the two
+// calls go to info_dev[0..1] (checked later by the caller).
+void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, double *out,
+                     int *info_dev) {
   if (k == 0) return;
   auto s = stream();
   const unsigned grid = (unsigned)std::min<int64_t>((dim * k + 255) / 256, 4096);
-  const unsigned long long key = (unsigned long long)(2 * group + side) << 40;
-  seed_matrix_kernel<<<grid, 256, 0, s>>>(out, (int)dim, (int)k, key);
+  shifted_identity_kernel<<<grid, 256, 0, s>>>(out, (int)dim, (int)k, (int)r);
   GQ_CUDA(cudaGetLastError());
-  auto bh = blas();
+  if (r == 0) return;
+  prof_begin(kProfSvdOrtho);
+  auto sh = solver();
   const int d = (int)dim, kk = (int)k, rr = (int)r;
-  const double one = 1.0, zero = 0.0, mone = -1.0;
-  if (r > 0) {
-    DevBuf t(r * k);
-    for (int pass = 0; pass < 2; ++pass) {
-      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, rr, kk, d, &one, vecs, d, out, d, &zero,
-                          t.p, rr));
-      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, d, kk, rr, &mone, vecs, d, t.p, rr, &one,
-                          out, d));
-    }
-  }
-  cholqr2(out, dim, k);
+  DevBuf a(dim * r), tau(r);
+  GQ_CUDA(cudaMemcpyAsync(a.p, vecs, sizeof(double) * dim * r, cudaMemcpyDeviceToDevice, s));
+  int lw1 = 0, lw2 = 0;
+  GQ_SOLVER(cusolverDnDgeqrf_bufferSize(sh, d, rr, a.p, d, &lw1));
+  GQ_SOLVER(cusolverDnDormqr_bufferSize(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, d, kk, rr, a.p, d,
+                                        tau.p, out, d, &lw2));
+  const int lw = std::max(lw1, lw2);
+  DevBuf work((int64_t)lw + 1);
+  GQ_SOLVER(cusolverDnDgeqrf(sh, d, rr, a.p, d, tau.p, work.p, lw, info_dev));
+  GQ_SOLVER(cusolverDnDormqr(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, d, kk, rr, a.p, d, tau.p, out, d,
+                             work.p, lw, info_dev + 1));
+  prof_end(kProfSvdOrtho, 0.0, 0.0);
 }
 
 struct Group {
@@ -390,6 +340,12 @@ struct Group {
   int64_t ev_off = 0, w_off = 0;  // gram: eigenvectors (dim x dim) and eigenvalues
   int64_t dim = 0;
   bool eig_m = true;              // gram: eigensolve on Theta Theta^T (else Theta^T Theta)
+  // Gram groups: the Gram matrix (gn x gn) at g_off; rank-revealing
+  // reduction (pcmgs.cu) with rank cap rcap: Q at q_off, T T^T at t_off;
+  // pc: the eigensolve ran on T T^T (rank r), eigenvectors Q Z at u_off
+  int64_t gn = 0, g_off = 0, q_off = 0, t_off = 0, u_off = 0;
+  int rcap = 0, r = -1;
+  bool pc = false;
   int64_t small_idx = -1;
   std::vector<double> svals;      // p values, descending
   std::vector<int> src_cols;      // source column of each value
@@ -470,10 +426,10 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       g.small_idx = n_small++;
     } else if (scale_side == 2) {
       g.route = kGramLeft;
-      g.eig_m = !transposed_gram(g.m, g.n);
+      g.eig_m = true;
     } else if (scale_side == 1) {
       g.route = kGramRight;
-      g.eig_m = transposed_gram(g.n, g.m);
+      g.eig_m = false;
     } else {
       g.route = kJacobi;
     }
@@ -576,27 +532,112 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
                                   lwork, jinfo.p + gi, prm));
     }
   }
-  // Gram groups: the canonical side's Gram matrix (eigenvalues in [0, |Theta|^2])
-  // in a slot padded to a bucket size with -1 on the extra diagonal, so the
-  // padding's eigenpairs sort below the real ones and stay in the padded
-  // coordinates; one batched eigensolve per bucket.
-  // Bucket sizes: multiples of 32 up to 64, of 64 above.  A batched
-  // eigensolve costs a few ms per call even for small matrices (GB300:
-  // 256 rows alone 7.6 ms, 16 of them 18 ms), so every group of at most 256
-  // rows joins one bucket padded to the largest of them.
+  // Gram groups.  Each group's canonical-side Gram matrix G (gn x gn,
+  // eigenvalues in [0, |Theta|^2]) is formed first; the rank-revealing
+  // reduction (pcmgs.cu) then finds its numerical range Q (gn x r) with
+  // Q^T G Q ~ T T^T.  A group whose rank stays within its cap solves the
+  // r x r matrix T T^T (eigenvectors Q Z); the others solve G itself.
+  // Either matrix goes into a slot padded to a bucket size with -1 on the
+  // extra diagonal, so the padding's eigenpairs sort below the real ones and
+  // stay in the padded coordinates; one batched eigensolve per bucket.
+  // Bucket sizes: 32 (cuSOLVER's batched Jacobi range), 64, one bucket for
+  // 65..256 padded to the largest of them, multiples of 64 above.
+  std::vector<Group *> gram;
+  int64_t gbuf_total = 0, q_total = 0, t_total = 0;
+  for (Group *g : groups)
+    if (g->route == kGramLeft || g->route == kGramRight) {
+      g->gn = g->eig_m ? g->m : g->n;
+      g->g_off = gbuf_total;
+      gbuf_total += g->gn * g->gn;
+      if (g->gn <= pcmgs_max_rows()) {
+        // rank cap: the reduction's cost grows as gn r^2 and the r x r
+        // eigensolve's as r^3, so beyond ~0.3 gn solving G directly is
+        // cheaper; a group whose smaller side is at most half the Gram
+        // dimension can always use its rank bound
+        const int64_t p = std::min(g->m, g->n);
+        int64_t cap = std::max<int64_t>(32, (3 * g->gn + 9) / 10);
+        if (2 * p <= g->gn) cap = std::max(cap, p);
+        g->rcap = (int)std::min<int64_t>(std::min<int64_t>(cap, g->gn), pcmgs_max_rank());
+        g->q_off = q_total;
+        q_total += g->gn * g->rcap;
+        g->t_off = t_total;
+        t_total += (int64_t)g->rcap * g->rcap;
+      }
+      gram.push_back(g);
+    }
+  DevBuf gbuf(gbuf_total), lbuf(q_total), qbuf(q_total), tbuf(t_total), cbuf(t_total);
+  prof_begin(kProfSvdGram);
+  {
+    const double one = 1.0, zero = 0.0;
+    for (Group *g : gram) {
+      const int m = (int)g->m, n = (int)g->n, gd = (int)g->gn;
+      const double *X = mats.p + g->mat_off;  // col-major n x m
+      double *G = gbuf.p + g->g_off;
+      if (2.0 * gd * gd * (double)(g->eig_m ? n : m) >= kTcMinFlops) {
+        // X is Theta row-major (m x n): Theta Theta^T contracts axis 1,
+        // Theta^T Theta axis 0
+        const int ax = g->eig_m ? 1 : 0;
+        dense_contract_tc(X, m, n, ax, X, m, n, ax, G);
+      } else if (g->eig_m) {  // Theta Theta^T = X^T X (m x m)
+        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, X, n, X, n, &zero, G, m));
+      } else {  // Theta^T Theta = X X^T (n x n)
+        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_T, n, n, m, &one, X, n, X, n, &zero, G, n));
+      }
+    }
+  }
+  prof_end(kProfSvdGram, 0.0, 0.0);
+  prof_begin(kProfSvdReduce);
+  {
+    std::vector<PcGroup> pcs[2];
+    std::vector<Group *> pcg[2];
+    for (Group *g : gram) {
+      if (g->rcap == 0) continue;
+      const int big = g->gn > kPcSmallRows ? 1 : 0;
+      pcs[big].push_back({g->g_off, g->q_off, g->t_off, (int)g->gn, g->rcap});
+      pcg[big].push_back(g);
+    }
+    if (!pcs[0].empty() || !pcs[1].empty()) {
+      DevArray<PcGroup> dg[2];
+      DevArray<int> dr[2];
+      for (int b = 0; b < 2; ++b) {
+        dg[b].upload(pcs[b]);
+        dr[b].upload(std::vector<int>(pcs[b].size(), -1));
+      }
+      launch_pcmgs(dg[0].p, (int)pcs[0].size(), dg[1].p, (int)pcs[1].size(), gbuf.p, lbuf.p,
+                   qbuf.p, tbuf.p, cbuf.p, dr[0].p, dr[1].p, kPcTol);
+      GQ_CUDA(cudaGetLastError());
+      std::vector<int> hr[2];
+      for (int b = 0; b < 2; ++b) {
+        hr[b].resize(pcs[b].size());
+        if (!hr[b].empty())
+          GQ_CUDA(cudaMemcpyAsync(hr[b].data(), dr[b].p, sizeof(int) * hr[b].size(),
+                                  cudaMemcpyDeviceToHost, s));
+      }
+      sync();
+      for (int b = 0; b < 2; ++b)
+        for (size_t i = 0; i < hr[b].size(); ++i) {
+          pcg[b][i]->r = hr[b][i];
+          pcg[b][i]->pc = hr[b][i] >= 0;
+        }
+    }
+  }
+  prof_end(kProfSvdReduce, 0.0, 0.0);
+  auto bucket_of = [](int64_t real) -> int64_t {
+    if (real <= 32) return 32;
+    if (real <= 64) return 64;
+    return (real + 63) / 64 * 64;
+  };
   std::map<int64_t, std::vector<Group *>> buckets;
-  int64_t small_dim = 0;
-  for (Group *g : groups)
-    if (g->route == kGramLeft || g->route == kGramRight) {
-      const int64_t real = g->eig_m ? g->m : g->n;
-      g->dim = real <= 64 ? (real + 31) / 32 * 32 : (real + 63) / 64 * 64;
-      if (g->dim <= 256) small_dim = std::max(small_dim, g->dim);
-    }
-  for (Group *g : groups)
-    if (g->route == kGramLeft || g->route == kGramRight) {
-      if (g->dim <= 256) g->dim = small_dim;
-      buckets[g->dim].push_back(g);
-    }
+  int64_t mid_dim = 0;
+  for (Group *g : gram) {
+    g->dim = (g->pc && g->r == 0) ? 0 : bucket_of(g->pc ? g->r : g->gn);
+    if (g->dim > 64 && g->dim <= 256) mid_dim = std::max(mid_dim, g->dim);
+  }
+  for (Group *g : gram) {
+    if (g->dim == 0) continue;  // a zero matrix: nothing to solve
+    if (g->dim > 64 && g->dim <= 256) g->dim = mid_dim;
+    buckets[g->dim].push_back(g);
+  }
   int64_t ev_total = 0, w_total = 0, n_gram = 0;
   for (auto &kv : buckets)
     for (Group *g : kv.second) {
@@ -610,38 +651,24 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   DevArray<int> einfo;
   if (n_gram > 0) {
     std::vector<PadDiagItem> pads;
+    std::vector<SlotItem> from_g, from_c;
     for (auto &kv : buckets)
-      for (Group *g : kv.second)
-        pads.push_back({g->ev_off, (int)g->dim, (int)(g->eig_m ? g->m : g->n)});
+      for (Group *g : kv.second) {
+        const int real = (int)(g->pc ? g->r : g->gn);
+        pads.push_back({g->ev_off, (int)g->dim, real});
+        if (g->pc)
+          from_c.push_back({g->t_off, g->ev_off, real, g->rcap, (int)g->dim});
+        else
+          from_g.push_back({g->g_off, g->ev_off, real, (int)g->gn, (int)g->dim});
+      }
     {
       DevArray<PadDiagItem> d;
       d.upload(pads);
       pad_diag_kernel<<<(unsigned)pads.size(), 256, 0, s>>>(d.p, ev.p);
       GQ_CUDA(cudaGetLastError());
     }
-    const double one = 1.0, zero = 0.0;
-    for (auto &kv : buckets)
-      for (Group *g : kv.second) {
-        const int m = (int)g->m, n = (int)g->n, bs = (int)g->dim;
-        const double *X = mats.p + g->mat_off;  // col-major n x m
-        const int gd = g->eig_m ? m : n;  // Gram dimension
-        if (2.0 * gd * gd * (double)(g->eig_m ? n : m) >= kTcMinFlops) {
-          // X is Theta row-major (m x n): Theta Theta^T contracts axis 1,
-          // Theta^T Theta axis 0; the symmetric result lands in the slot
-          DevBuf gm((int64_t)gd * gd);
-          const int ax = g->eig_m ? 1 : 0;
-          dense_contract_tc(X, m, n, ax, X, m, n, ax, gm.p);
-          GQ_CUDA(cudaMemcpy2DAsync(ev.p + g->ev_off, sizeof(double) * bs, gm.p,
-                                    sizeof(double) * gd, sizeof(double) * gd, gd,
-                                    cudaMemcpyDeviceToDevice, s));
-        } else if (g->eig_m) {  // Theta Theta^T = X^T X (m x m)
-          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, X, n, X, n, &zero,
-                              ev.p + g->ev_off, bs));
-        } else {  // Theta^T Theta = X X^T (n x n)
-          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_T, n, n, m, &one, X, n, X, n, &zero,
-                              ev.p + g->ev_off, bs));
-        }
-      }
+    launch_items(slot_copy_kernel, from_g, gbuf.p, ev.p);
+    launch_items(slot_copy_kernel, from_c, cbuf.p, ev.p);
     // One batched eigensolve per bucket.  The solves are latency-bound (a
     // 1486-row syevd is ~60 ms of small launches), so buckets of different
     // sizes run side by side: largest first, dealt round-robin over the
@@ -710,6 +737,26 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
             einfo.p + v.io, v.nb));
     }
   }
+  // eigenvectors of the reduced groups: U = Q Z (gn x r), Z the slot's
+  // last r columns (ascending eigenvalues, padded coordinates zero)
+  int64_t u_total = 0;
+  for (Group *g : gram)
+    if (g->pc && g->r > 0) {
+      g->u_off = u_total;
+      u_total += g->gn * g->r;
+    }
+  DevBuf ubuf(u_total);
+  {
+    const double one = 1.0, zero = 0.0;
+    for (Group *g : gram) {
+      if (!g->pc || g->r == 0) continue;
+      const int gd = (int)g->gn, r = g->r, bs = (int)g->dim;
+      // Q row-major gn x rcap is col-major rcap x gn: op(A) = A^T
+      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, gd, r, r, &one, qbuf.p + g->q_off, g->rcap,
+                          ev.p + g->ev_off + (int64_t)(bs - r) * bs, bs, &zero,
+                          ubuf.p + g->u_off, gd));
+    }
+  }
   prof_end(kProfSvdEig, 0.0, 0.0);
   // ---- values to the host ---------------------------------------------------
   std::vector<double> hs_small(n_small * kSmall), hs_j(js_total), hw(w_total);
@@ -756,6 +803,22 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       for (int64_t j = 0; j < g->p; ++j) {
         g->src_cols[j] = (int)j;
         g->svals[j] = hs_j[g->sv_off + j];
+      }
+    } else if (g->pc) {
+      // reduced group: r Ritz values (the slot's last r), zeros beyond; the
+      // j-th largest has eigenvector column r - 1 - j of U = Q Z
+      const int64_t r = g->r;
+      const double *lam = r > 0 ? hw.data() + g->w_off : nullptr;  // ascending
+      const double lmax = r > 0 ? std::max(lam[g->dim - 1], 0.0) : 0.0;
+      for (int64_t j = 0; j < g->p; ++j) {
+        if (j < r) {
+          g->src_cols[j] = (int)(r - 1 - j);
+          const double l = lam[g->dim - 1 - j];
+          g->svals[j] = (l > kGramZeroRtol * lmax) ? std::sqrt(l) : 0.0;
+        } else {
+          g->src_cols[j] = 0;
+          g->svals[j] = 0.0;
+        }
       }
     } else {
       const double *lam = hw.data() + g->w_off;  // ascending
@@ -834,13 +897,15 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   GQ_CUDA(cudaMemsetAsync(Lb.p, 0, sizeof(double) * L_total, s));
   GQ_CUDA(cudaMemsetAsync(Rb.p, 0, sizeof(double) * R_total, s));
   const bool scale_l = scale_side == 1, scale_r = scale_side == 2;
-  std::vector<ColItem> l_small, r_small, l_jac, r_jac, l_ev, r_ev;
-  // A Gram route whose eigensolve ran on the canonical side supplies that
-  // side's columns for kept zero values too: the eigenvectors of the
-  // zero (below-floor) eigenvalues are orthonormal and orthogonal to the
-  // kept nonzero ones, which is all the completion has to provide.
+  std::vector<ColItem> l_small, r_small, l_jac, r_jac, l_ev, r_ev, l_pc, r_pc;
+  // A Gram group solved in full supplies the canonical side's columns for
+  // kept zero values too: the eigenvectors of the zero (below-floor)
+  // eigenvalues are orthonormal and orthogonal to the kept nonzero ones,
+  // which is all the completion has to provide.  A reduced group has no
+  // such vectors and takes the canonical completion.
   auto eig_is_canonical = [](const Group *g) {
-    return (g->route == kGramLeft && g->eig_m) || (g->route == kGramRight && !g->eig_m);
+    return !g->pc &&
+           ((g->route == kGramLeft && g->eig_m) || (g->route == kGramRight && !g->eig_m));
   };
   for (Group *g : groups) {
     const int64_t ncopy = eig_is_canonical(g) ? g->keep : g->keep_nz;
@@ -860,10 +925,16 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
         }
         case kGramLeft:
         case kGramRight:
-          if (g->eig_m)
+          if (g->pc) {
+            if (g->eig_m)
+              l_pc.push_back({g->u_off, g->L_off, (int)g->m, (int)g->gn, (int)g->m, sc, (int)j, 1.0});
+            else
+              r_pc.push_back({g->u_off, g->R_off, (int)g->n, (int)g->gn, (int)g->n, sc, (int)j, 1.0});
+          } else if (g->eig_m) {
             l_ev.push_back({g->ev_off, g->L_off, (int)g->m, (int)g->dim, (int)g->m, sc, (int)j, 1.0});
-          else
+          } else {
             r_ev.push_back({g->ev_off, g->R_off, (int)g->n, (int)g->dim, (int)g->n, sc, (int)j, 1.0});
+          }
           break;
       }
     }
@@ -874,9 +945,10 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   launch_items(col_copy_kernel, r_jac, jr.p, Rb.p);
   launch_items(col_copy_kernel, l_ev, ev.p, Lb.p);
   launch_items(col_copy_kernel, r_ev, ev.p, Rb.p);
+  launch_items(col_copy_kernel, l_pc, ubuf.p, Lb.p);
+  launch_items(col_copy_kernel, r_pc, ubuf.p, Rb.p);
   // projections for the Gram routes: R = X L (canonical left) or L = X^T R
-  // (canonical right); a transposed route first builds the canonical factor
-  // from the other side's eigenvectors (L = qr(X^T R) or R = qr(X L))
+  // (canonical right)
   {
     const double one = 1.0, zero = 0.0;
     for (Group *g : groups) {
@@ -900,25 +972,10 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
           GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, &one, X, n, L, m, &zero, R,
                               n));
       };
-      if (g->route == kGramLeft) {
-        if (!g->eig_m) {
-          left_from_right();
-          prof_begin(kProfSvdOrtho);
-          normalise_columns(L, m, k);
-          cholqr2(L, m, k);
-          prof_end(kProfSvdOrtho, 0.0, 0.0);
-        }
+      if (g->route == kGramLeft)
         right_from_left();
-      } else {
-        if (g->eig_m) {
-          right_from_left();
-          prof_begin(kProfSvdOrtho);
-          normalise_columns(R, n, k);
-          cholqr2(R, n, k);
-          prof_end(kProfSvdOrtho, 0.0, 0.0);
-        }
+      else
         left_from_right();
-      }
     }
   }
   // sign convention on the kept nonzero columns (by the left factor)
@@ -934,7 +991,16 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       GQ_CUDA(cudaGetLastError());
     }
   }
-  // canonical completion of the kept zero values on the orthonormal side(s)
+  // canonical completion of the kept zero values on the orthonormal side(s);
+  // their status words are checked once, after the output scatter
+  DevArray<int> cinfo;
+  {
+    int64_t ncomp = 0;
+    for (Group *g : groups)
+      if (g->keep > g->keep_nz) ncomp += 2;
+    cinfo.upload(std::vector<int>(2 * ncomp + 2, 0));
+  }
+  int64_t cslot = 0;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     Group *g = groups[gi];
     const int64_t kz = g->keep - g->keep_nz;
@@ -944,22 +1010,17 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       DevBuf q(std::max<int64_t>(dim * g->nnz, 1));
       std::vector<ColItem> items;
       const bool gram = g->route == kGramLeft || g->route == kGramRight;
-      if (gram && g->eig_m != left) {
-        // transposed route: every nonzero value is kept (a zero is), so the
-        // canonical factor's first nnz columns are the nonzero vectors
-        null_completion(left ? Lb.p + g->L_off : Rb.p + g->R_off, dim, g->nnz, kz, (int)gi,
-                        left ? 0 : 1, dst);
-        return;
-      }
       for (int64_t j = 0; j < g->nnz; ++j)
-        items.push_back({gram ? g->ev_off : (left ? g->lv_off : g->rv_off), 0, (int)dim,
-                         gram ? (int)g->dim : (left ? g->ld_l : g->ld_r), (int)dim,
-                         g->src_cols[j], (int)j, 1.0});
-      const double *src = gram ? ev.p
+        items.push_back({gram ? (g->pc ? g->u_off : g->ev_off) : (left ? g->lv_off : g->rv_off),
+                         0, (int)dim,
+                         gram ? (int)(g->pc ? g->gn : g->dim) : (left ? g->ld_l : g->ld_r),
+                         (int)dim, g->src_cols[j], (int)j, 1.0});
+      const double *src = gram ? (g->pc ? ubuf.p : ev.p)
                                : g->route == kSmallJacobi ? (left ? sv.p : su.p)
                                                           : (left ? jl.p : jr.p);
       launch_items(col_copy_kernel, items, src, q.p);
-      null_completion(q.p, dim, g->nnz, kz, (int)gi, left ? 0 : 1, dst);
+      null_completion(q.p, dim, g->nnz, kz, dst, cinfo.p + cslot);
+      cslot += 2;
     };
     if (eig_is_canonical(g)) continue;  // zero columns came with the eigenvectors
     if (scale_side != 1) completion(true, Lb.p + g->L_off + g->keep_nz * g->m);
@@ -1023,6 +1084,14 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     scatter_kernel<<<(unsigned)items.size(), 256, 0, s>>>(d.p, Lb.p, Rb.p, out.u->data.p,
                                                          out.vt->data.p);
     GQ_CUDA(cudaGetLastError());
+  }
+  if (cslot > 0) {
+    std::vector<int> hinfo(cslot, 0);
+    GQ_CUDA(cudaMemcpyAsync(hinfo.data(), cinfo.p, sizeof(int) * cslot, cudaMemcpyDeviceToHost,
+                            s));
+    sync();
+    for (int v : hinfo)
+      if (v != 0) fail(kSolverError, "QR of a null-space completion failed");
   }
   prof_end(kProfSvd, 0.0, 0.0);
   return out;

@@ -363,44 +363,24 @@ def select_kept(all_s: np.ndarray, trunc_err: float, dmin: int, dmax: int):
     return order, D, err
 
 
-_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
-
-
-def completion_seed_matrix(group: int, side: int, dim: int, k: int) -> np.ndarray:
-    """dim x k matrix of counter-based pseudo-random numbers in [-0.5, 0.5):
-    element (i, j) = splitmix64(((2*group + side) << 40) ^ (i << 20) ^ j),
-    top 53 bits scaled by 2^-53, minus 0.5 (bit-identical on the GPU)."""
-    i = np.arange(dim, dtype=np.uint64)[:, None]
-    j = np.arange(k, dtype=np.uint64)[None, :]
-    with np.errstate(over="ignore"):
-        x = (np.uint64((2 * group + side) << 40)) ^ (i << np.uint64(20)) ^ j
-        z = x + np.uint64(0x9E3779B97F4A7C15)
-        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-        z = z ^ (z >> np.uint64(31))
-    return (z >> np.uint64(11)).astype(np.float64) * (2.0 ** -53) - 0.5
-
-
 def null_completion(q_nz: np.ndarray, dim: int, k: int, group: int = 0,
                     side: int = 0) -> np.ndarray:
-    """``k`` orthonormal vectors orthogonal to the orthonormal columns of
-    ``q_nz`` (``dim x r``): the seed matrix of :func:`completion_seed_matrix`
-    projected off ``q_nz`` twice (classical Gram-Schmidt with
-    re-orthogonalisation) and orthonormalised by CholeskyQR2 (Cholesky
-    factors with a positive diagonal).  The result does not depend on the
-    signs of the columns of ``q_nz``."""
+    """``k`` orthonormal vectors orthogonal to the ``r`` orthonormal columns
+    of ``q_nz`` (``dim x r``): columns ``r .. r+k-1`` of the orthogonal
+    factor of the complete Householder QR of ``q_nz`` (LAPACK ``dgeqrf`` +
+    ``dorgqr`` conventions), i.e. the unit vectors e_r .. e_{r+k-1} carried
+    through the r reflectors -- the basis states of the group that the
+    nonzero vectors leave, made orthogonal to them.  O(dim r (r + k)) work;
+    exactly orthonormal whatever the overlap of the unit vectors with
+    ``q_nz``.  With r = 0 it is the first k unit vectors.  (``group`` and
+    ``side`` do not enter.)"""
     if k == 0:
         return np.zeros((dim, 0))
-    w = completion_seed_matrix(group, side, dim, k)
     r = q_nz.shape[1]
-    if r > 0:
-        for _ in range(2):
-            w = w - q_nz @ (q_nz.T @ w)
-    for _ in range(2):
-        g = w.T @ w
-        lo = np.linalg.cholesky(g)
-        w = np.linalg.solve(lo, w.T).T   # w L^{-T}
-    return np.ascontiguousarray(w)
+    if r == 0:
+        return np.eye(dim, k)
+    qf = np.linalg.qr(q_nz, mode="complete")[0]
+    return np.ascontiguousarray(qf[:, r:r + k])
 
 
 def svd(t: BSTensor, ldims: int, ldiv, trunc_err: float, dmin: int, dmax: int) -> SVDResult:
