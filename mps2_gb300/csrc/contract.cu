@@ -187,7 +187,7 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
         max_k = std::max(max_k, k);
       }
     }
-    if (skinny_eligible(b, max_k, max_n)) {
+    if (skinny_eligible(b, max_k, max_n) && (int)free_a.size() <= skinny_max_free_legs()) {
       auto strides = [](const Tensor &t, int64_t blk, int64_t *str) {
         int64_t s = 1;
         for (int l = t.rank() - 1; l >= 0; --l) {
@@ -286,14 +286,18 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
       const double frac = tc_frac >= 0.0 ? tc_frac : (prec == kTF32x3 ? 0.02 : 0.03);
       plan->tc_frac = frac;
       double useful = 0.0, padded = 0.0;
+      int64_t ksum = 0;
       for (auto &cp : kv.second) {
         int64_t k = 1;
         for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
         useful += 2.0 * m * n * k;
         padded += 2.0 * (double)((m + TM - 1) / TM * TM) * (double)((n + TN - 1) / TN * TN) *
                   ((k + 31) / 32 * 32.0);
+        ksum += (k + 31) / 32 * 32;
       }
       tc = useful >= frac * padded;
+      // the FP64-accurate kernel's exact running sums cover k <= oz_max_k()
+      if (prec == kFP64TC && ksum > oz_max_k()) tc = false;
       if (tc) plan->padded_flops += padded;
     }
     any_tc |= tc;

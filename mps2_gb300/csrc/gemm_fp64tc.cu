@@ -18,17 +18,26 @@
 //    partial sum of the g <= 3 accumulators is an integer below 2^24 times
 //    2^(-8g), i.e. exact in FP32.  The shared g >= 4 accumulator rounds at
 //    2^-24 of a value already 2^-32 below the leading one;
-//  * every 256 k the accumulators are read out, added in FP64 (smallest
-//    order first) and accumulated into the output tile, which is finally
-//    scaled by 2^(E_i + F_j - 14).
+//  * every 256 k the accumulators are read out and folded into an exact
+//    64-bit integer running sum on the grid 2^-30 (in units of the leading
+//    digit product): the orders 0..3 are integers times 2^(-8g), so their
+//    values times 2^30 are exact integers; the shared order 4..6
+//    accumulator is rounded to that grid (2^-31, below FP64 rounding of the
+//    result).  No FP64 arithmetic happens per chunk -- GB300's FP64 rate
+//    would make the merge, not the tensor cores, the bottleneck -- only one
+//    conversion per output element at the end, where the tile is scaled by
+//    2^(E_i + F_j - 14) and written once, through shared memory in whole
+//    rows.  A tile's k (summed over its block pairs) is at most 2^16, so the
+//    integer sum stays below 2^63.
 // Result: error about 2^-55 * max|a_i.| * max|b_.j| per product term, the
 // same order as an FP64 GEMM's.
 //
 // Tiles are 128 x 96 (5 accumulators x 96 columns = 480 of TMEM's 512), the
 // k-step is 32 bf16 (64-byte rows, 64-byte swizzle), two pipeline stages of
-// 7 A and 7 B slice images (98 KB each).  CTA layout as in the 3xTF32
-// kernel: warps 0-3 merge and write back, warp 4 issues bulk copies, warp 5
-// owns TMEM and issues the MMAs; every wait is bounded.
+// 7 A and 7 B slice images (98 KB each).  CTA layout: warps 0-7 merge and
+// write back (warp w reads TMEM lanes 32 (w % 4) .. +31, columns
+// 48 (w / 4) .. +47), warp 8 issues bulk copies, warp 9 owns TMEM and
+// issues the MMAs; every wait is bounded.
 #include <cstdint>
 #include <map>
 
@@ -48,7 +57,9 @@ constexpr int kAStage = kSlices * kATile;     // 56 KB
 constexpr int kBStage = kSlices * kBTile;     // 42 KB
 constexpr int kStageBytes = kAStage + kBStage;
 constexpr int kChunkSteps = 8;                // 256 k between read-outs
-constexpr int kThreads = 192;
+constexpr int kThreads = 320;          // 8 merge warps, producer, MMA issuer
+constexpr int kMergeThreads = 256;
+constexpr int kMaxK = 1 << 16;          // k of one tile, summed over its pairs
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000ll;
 constexpr int kNoExp = -(1 << 30);            // column outside the tile
@@ -271,16 +282,13 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
           smem_u32(bar))
       : "memory");
 }
-#define OZ_LD32(taddr, r)                                                                     \
+#define OZ_LD16(taddr, r)                                                                     \
   asm volatile(                                                                               \
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
-      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"      \
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
+      "%14,%15}, [%16];"                                                                      \
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),   \
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),            \
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),         \
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),         \
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),         \
-        "=r"(r[31])                                                                           \
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])                                                 \
       : "r"(taddr))
 __device__ __forceinline__ void tc_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -326,13 +334,13 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
       mbar_init(&sm.empty[s], 1);
     }
     mbar_init(&sm.accfull, 1);
-    mbar_init(&sm.accempty, 128);
+    mbar_init(&sm.accempty, oz::kMergeThreads);
     mbar_init(&sm.mma_done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   for (int j = threadIdx.x; j < oz::BN; j += blockDim.x)
     sm.colexp[j] = (t.col0 + j < t.n) ? rowexp_b[t.b_rbase + t.col0 + j] : oz::kNoExp;
-  if (warp == 5) {
+  if (warp == 9) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&sm.tmem_base)),
                  "r"(oz::kTmemCols)
@@ -345,7 +353,7 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
   const uint32_t tmem = sm.tmem_base;
   const int nchunks = sm.nchunks, nsteps = sm.nsteps;
 
-  if (warp == 4) {
+  if (warp == 8) {
     // ---------------- producer -------------------------------------------------
     if (lane == 0) {
       int stage = 0;
@@ -370,7 +378,7 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
         mbar_wait(&sm.full[st % oz::kStages], (uint32_t)(st / oz::kStages) & 1u, &no_abort);
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     // ---------------- MMA issuer -------------------------------------------------
     if (lane == 0) {
       constexpr uint32_t idesc = make_idesc_bf16(oz::BM, oz::BN);
@@ -422,63 +430,68 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
       mbar_wait(&sm.mma_done, 0u, &no_abort);
     }
   } else {
-    // ---------------- merge warps 0-3 --------------------------------------------
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-    const int row = t.row0 + warp * 32 + lane;
-    double *crow = C + t.c_off + (int64_t)row * t.n;
-    const int er = (row < t.m) ? rowexp_a[t.a_rbase + row] : oz::kNoExp;
-    for (int c = 0; c < nchunks; ++c) {
-      if (!mbar_wait(&sm.accfull, (uint32_t)c & 1u, abort)) break;
-      fence_after_sync();
-      const bool last = c + 1 == nchunks;
-#pragma unroll 1
-      for (int cb = 0; cb < oz::BN / 32; ++cb) {
-        double v[32];
+    // ---------------- merge warps 0-7 --------------------------------------------
+    const int quad = warp & 3, half = warp >> 2;
+    const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
+    const int lrow = quad * 32 + lane;          // row within the tile
+    const int cbase = half * (oz::BN / 2);      // first of this thread's 48 columns
+    long long run[oz::BN / 2];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = 0.0;
+    for (int j = 0; j < oz::BN / 2; ++j) run[j] = 0;
+    const float two30 = 1073741824.0f;
+    bool done = true;
+    for (int c = 0; c < nchunks; ++c) {
+      if (!mbar_wait(&sm.accfull, (uint32_t)c & 1u, abort)) { done = false; break; }
+      fence_after_sync();
+#pragma unroll
+      for (int cb = 0; cb < oz::BN / 2 / 16; ++cb) {
 #pragma unroll 1
-        for (int a = oz::kAcc - 1; a >= 0; --a) {
-          uint32_t f[32];
-          OZ_LD32(tmem + lane_base + (uint32_t)(a * oz::BN + cb * 32), f);
+        for (int a = 0; a < oz::kAcc; ++a) {
+          uint32_t f[16];
+          OZ_LD16(tmem + lane_base + (uint32_t)(a * oz::BN + cbase + cb * 16), f);
           tc_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) v[j] += (double)__uint_as_float(f[j]);
-        }
-        if (row < t.m) {
-          // all 32 loads of the running sums first (independent, in flight
-          // together), then the adds and stores
-          const int cbase = t.col0 + cb * 32;
-          if (c > 0) {
-            double old[32];
-#pragma unroll
-            for (int j = 0; j < 32; ++j) old[j] = (cbase + j < t.n) ? crow[cbase + j] : 0.0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] += old[j];
-          }
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int cl = cb * 32 + j, col = cbase + j;
-            if (col < t.n) {
-              double x = v[j];
-              if (last) {
-                const int ec = sm.colexp[cl];
-                x = (oz::valid_exp(er) && oz::valid_exp(ec)) ? ldexp(x, er + ec - 14) : 0.0;
-              }
-              crow[col] = x;
-            }
+          for (int j = 0; j < 16; ++j) {
+            // orders 0..3: x * 2^30 is an exact integer; order 4..6: rounded
+            const float x = __uint_as_float(f[j]) * two30;
+            run[cb * 16 + j] += a < oz::kAcc - 1 ? __float2ll_rz(x) : __float2ll_rn(x);
           }
         }
       }
       fence_before_sync();
       mbar_arrive(&sm.accempty);
     }
-    if (!*abort && nchunks == 0 && row < t.m)
-      for (int j = 0; j < oz::BN && t.col0 + j < t.n; ++j) crow[t.col0 + j] = 0.0;
+    // all MMAs are complete (the last chunk's accumulators were read), so
+    // the pipeline stages are free: stage the scaled tile there and write
+    // whole rows (after an abort copies may still be landing there: nothing
+    // is staged)
+    double *tile = reinterpret_cast<double *>(sm.stage[0]);  // 128 x 96
+    const int row = t.row0 + lrow;
+    const int er = (row < t.m) ? rowexp_a[t.a_rbase + row] : oz::kNoExp;
+    if (done) {
+#pragma unroll
+      for (int j = 0; j < oz::BN / 2; ++j) {
+        const int cl = cbase + j;
+        const int ec = sm.colexp[cl];
+        double x = 0.0;
+        if (nchunks > 0 && oz::valid_exp(er) && oz::valid_exp(ec))
+          x = ldexp((double)run[j], er + ec - 44);
+        tile[lrow * oz::BN + cl] = x;
+      }
+    }
+    asm volatile("bar.sync 1, %0;" ::"n"(oz::kMergeThreads) : "memory");
+    if (done && !*abort) {
+      const int rows = min(oz::BM, t.m - t.row0), cols = min(oz::BN, t.n - t.col0);
+      for (int e = threadIdx.x; e < rows * cols; e += oz::kMergeThreads) {
+        const int r = e / cols, cl = e % cols;
+        C[t.c_off + (int64_t)(t.row0 + r) * t.n + t.col0 + cl] = tile[r * oz::BN + cl];
+      }
+    }
   }
 
   fence_before_sync();
   __syncthreads();
-  if (warp == 5) {
+  if (warp == 9) {
     fence_after_sync();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(oz::kTmemCols)
@@ -495,6 +508,7 @@ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // ---------------------------------------------------------------------------
 int oz_tile_m() { return oz::BM; }
 int oz_tile_n() { return oz::BN; }
+int64_t oz_max_k() { return oz::kMaxK; }
 
 void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
                    const std::vector<int> &k_legs, int tile_rows, OzPackPlan &pp) {
