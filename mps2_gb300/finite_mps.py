@@ -227,3 +227,68 @@ def DirectStateInitMps(mps: FiniteMPS, stat_labs: Sequence[int], zero_div) -> No
     mps[N - 1] = t
     mps.center = 0
     mps.tens_cano_type = [FiniteMPS.NONE] + [FiniteMPS.RIGHT] * (N - 1)
+
+
+def extend_direct_random_tensors(mps: FiniteMPS, stat_labs_set: Sequence[Sequence[int]],
+                                 zero_div, enlarged_dim: int, seed: int = 0) -> List[GQTensor]:
+    """The site tensors of ``ExtendDirectRandomInitMps``
+    (``finite_mps_init.h:269-330``) before its final ``Centralize(0)``: a
+    sum of the product states ``stat_labs_set[j]``, each bond carrying one
+    sector of dimension ``enlarged_dim`` per product state (the charge that
+    product state puts on that bond), every allowed block filled with random
+    values.  The head tensor carries the total charge of the first product
+    state.  GraceQ/tensor's ``Random`` (its generator and distribution) is
+    not in the reference tree; this uses numpy's PCG64 seeded with ``seed``
+    and values uniform in [0, 1)."""
+    zero_div = QN(zero_div)
+    N = mps.size()
+    nfuse = len(stat_labs_set)
+    if nfuse < 1:
+        raise ValueError("at least one product state")
+    if any(len(labs) != N for labs in stat_labs_set):
+        raise ValueError("one state label per site in every product state")
+    if enlarged_dim < 1:
+        raise ValueError("enlarged_dim must be positive")
+    rng = np.random.default_rng(seed)
+    pb = mps.site_vec.sites
+
+    def random_fill(t: GQTensor) -> GQTensor:
+        for c in t.allowed_coords(t.div):
+            t.blocks[c] = rng.random(t.block_shape(c))
+        return t
+
+    div = pb[0].qn_of_coor(stat_labs_set[0][0])
+    for i in range(1, N):
+        div = div + pb[i].qn_of_coor(stat_labs_set[0][i])
+    rq = [div - pb[0].qn_of_coor(stat_labs_set[j][0]) for j in range(nfuse)]
+    rvb = Index([(q, enlarged_dim) for q in rq], OUT)
+    tens = [random_fill(GQTensor([pb[0], rvb], div))]
+    for i in range(1, N - 1):
+        lvb = rvb.inverse()
+        # lvb's sector j (coordinate j * enlarged_dim) carries product state j
+        rq = [zero_div - pb[i].qn_of_coor(stat_labs_set[j][i]) +
+              lvb.qn_of_coor(j * enlarged_dim) for j in range(nfuse)]
+        rvb = Index([(q, enlarged_dim) for q in rq], OUT)
+        tens.append(random_fill(GQTensor([lvb, pb[i], rvb], zero_div)))
+    tens.append(random_fill(GQTensor([rvb.inverse(), pb[N - 1]], zero_div)))
+    return tens
+
+
+def ExtendDirectRandomInitMps(mps: FiniteMPS, stat_labs_set: Sequence[Sequence[int]], zero_div,
+                              enlarged_dim: int, seed: int = 0) -> None:
+    """``ExtendDirectRandomInitMps`` (``finite_mps_init.h:269-330``): the
+    random sum of product states of :func:`extend_direct_random_tensors`,
+    centralised at site 0 on the GPU, the head tensor normalised."""
+    tens = extend_direct_random_tensors(mps, stat_labs_set, zero_div, enlarged_dim, seed)
+    for i, t in enumerate(tens):
+        mps[i] = t
+    mps.Centralize(0)
+    t0 = mps[0]
+    nrm = float(np.sqrt(sum(float(np.sum(b * b)) for b in t0.blocks.values())))
+    if nrm > 0.0:
+        for k in t0.blocks:
+            t0.blocks[k] = t0.blocks[k] / nrm
+    # the reference normalises through the writing accessor, which marks the
+    # site non-canonical and the MPS uncentralised
+    mps.tens_cano_type[0] = FiniteMPS.NONE
+    mps.center = kUncentralizedCenterIdx

@@ -84,6 +84,21 @@ def j1j2_cylinder_pairs(Lx: int, Ly: int, J1: float, J2: float):
 # ---------------------------------------------------------------------------
 # Hubbard with U(1)xU(1) (N_up, N_dn), basis {0, up, dn, updn}
 # ---------------------------------------------------------------------------
+def kitaev_simple_pairs(Nx: int = 4, Ny: int = 2):
+    """The zz bonds of the ``2DKitaevSimpleCase`` lattice
+    (``test_two_site_update_finite_vmps.cc:311-325``): for every odd column
+    x and every y, the bond between honeycomb sites (x, y) and
+    (x - 1, y + 1), site index Ny * (x mod Nx) + (y mod Ny), ordered."""
+    pairs = []
+    for x in range(Nx):
+        for y in range(Ny):
+            if x % 2 == 1:
+                s0 = Ny * (x % Nx) + y % Ny
+                s1 = Ny * ((x - 1) % Nx) + (y + 1) % Ny
+                pairs.append((min(s0, s1), max(s0, s1), 1.0))
+    return pairs
+
+
 def hubbard_ops():
     """Operators of ``test_two_site_update_finite_vmps.cc:796-859``."""
     pb_out = Index([(QN(0, 0), 1), (QN(1, 0), 1), (QN(0, 1), 1), (QN(1, 1), 1)], OUT)

@@ -316,3 +316,21 @@ def test_two_site_finite_vmps_file_contract(lib, tmp_path):
     assert os.path.exists(os.path.join(sp.temp_path, "renv1.gqten"))
     e1 = TwoSiteFiniteVMPS(mps, mpo, sp)   # resumes from temp_path
     assert abs(e1 - golden) <= tol and mps.empty()
+
+
+def test_dmrg_kitaev_extend_direct_random_init_gpu(lib):
+    """``2DKitaevSimpleCase`` (``test_two_site_update_finite_vmps.cc:311-345``)
+    through the product's ``ExtendDirectRandomInitMps`` (random sum of the two
+    Neel states, centralised on the GPU): golden energy -1.0 within 1e-12."""
+    from mps2_gb300.finite_mps import ExtendDirectRandomInitMps
+    from mps2_gb300.vmps import DMRGState, LanczosParams, SweepParams
+    from test_oracle_golden import kitaev_case
+    sv, mpo, qn0, labs, p, golden, tol = kitaev_case()
+    mps = FiniteMPS(sv)
+    ExtendDirectRandomInitMps(mps, labs, qn0, 2, seed=0)
+    assert mps.GetCenter() != 0 and mps.GetTenCanoType(0) == FiniteMPS.NONE
+    assert all(mps.GetTenCanoType(i) == FiniteMPS.RIGHT for i in range(1, len(mps)))
+    st = DMRGState(mps.tens, mpo)
+    st.init_envs("fp64")
+    e0, _ = st.sweep(SweepParams(p[0], p[1], p[2], p[3], LanczosParams(p[4], p[5])))
+    assert abs(e0 - golden) <= tol, e0

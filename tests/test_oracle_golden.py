@@ -89,3 +89,51 @@ def test_oracle_lanczos_vs_dense(params):
     assert np.allclose(Hd, Hd.T)
     e_dense = np.linalg.eigvalsh(Hd)[0]
     assert abs(res.gs_eng - e_dense) <= 1e-8
+
+
+def kitaev_case():
+    """``2DKitaevSimpleCase`` (``test_two_site_update_finite_vmps.cc:311-345``):
+    the honeycomb zz model on 4 x 2 sites from the random sum of the two Neel
+    product states (``ExtendDirectRandomInitMps`` with enlarged dimension 2),
+    4 sweeps, D=8, truncation error 1e-4, Lanczos tolerance 1e-10; golden
+    energy -1.0 (tolerance 1e-12)."""
+    from mps2_gb300 import hamiltonians as H
+    N = 8
+    sv, mpo, qn0, _ = H.heisenberg_pairs(N, H.kitaev_simple_pairs(4, 2), ising_only=True)
+    labs = [[i % 2 for i in range(N)], [(i + 1) % 2 for i in range(N)]]
+    return sv, mpo, qn0, labs, (4, 8, 8, 1e-4, 1e-10, 200), -1.0, 1e-12
+
+
+def test_oracle_kitaev_extend_direct_random_init():
+    import oracle.finite_mps as ofm
+    from mps2_gb300.finite_mps import extend_direct_random_tensors
+    sv, mpo, qn0, labs, p, golden, tol = kitaev_case()
+    mps = FiniteMPS(sv)
+    tens = [to_oracle(t) for t in extend_direct_random_tensors(mps, labs, qn0, 2, seed=0)]
+    cano = [0] * len(tens)
+    ofm.centralize(tens, cano, 0)
+    nrm = np.sqrt(sum(float(np.sum(b * b)) for b in tens[0].blocks.values()))
+    for k in tens[0].blocks:
+        tens[0].blocks[k] = tens[0].blocks[k] / nrm
+    sp = SweepParams(p[0], p[1], p[2], p[3], LanczosParams(p[4], p[5]))
+    e0 = oracle.two_site_finite_vmps(tens, [to_oracle(t) for t in mpo], sp)
+    assert abs(e0 - golden) <= tol, e0
+
+
+def test_extend_direct_random_tensors_structure():
+    """Each bond carries one sector of the enlarged dimension per product
+    state, with that product state's bond charge (as DirectStateInitMps
+    computes it); every tensor has the reference's divergences."""
+    from mps2_gb300.finite_mps import extend_direct_random_tensors
+    sv, mpo, qn0, labs, *_ = kitaev_case()
+    mps = FiniteMPS(sv)
+    tens = extend_direct_random_tensors(mps, labs, qn0, 2, seed=3)
+    for j, lab in enumerate(labs):
+        d = FiniteMPS(sv)
+        DirectStateInitMps(d, lab, qn0)
+        for i in range(len(tens) - 1):
+            rvb = tens[i].indices[-1]
+            assert rvb.dims[j] == 2
+            assert rvb.qns[j] == d.tens[i].indices[-1].qns[0]
+    assert all(t.div == qn0 for t in tens[1:])
+    assert all(t.blocks for t in tens)
