@@ -1,34 +1,43 @@
 #!/usr/bin/env python
 """Benchmark: two-site finite DMRG sweep on one GB300.
 
-Workload (the configuration the headline metric is quoted on): spin-1/2
-Heisenberg open chain, L=100, J=1, U(1) Sz, total Sz=0, Neel product state
-with a seed-0 shuffled site order; the bond dimension grows
-500 -> 800 -> 1100 -> 1400 -> 1700 -> 2000 (one sweep each), Lanczos tolerance
-1e-10.  The growth sweeps up to 1700 prepare the state (untimed); then
-``--warmup`` sweeps and ``--steps`` timed sweeps run at D=2000.
+Workload (the configuration the headline metric is quoted on): 1D Fermi-
+Hubbard open chain, L=64, t=1, U=8, half filling (32 up, 32 down), total
+Sz=0, U(1)xU(1) (N, Sz) quantum numbers, physical dimension 4 with
+Jordan-Wigner fermion signs, MPO bond dimension 6; alternating up/down
+product state; the bond dimension grows 1000 -> 1430 -> ... -> 4000 over 8
+sweeps (untimed set-up), Lanczos tolerance 1e-10 (100 iterations at most).
+Then ``--warmup`` sweeps and ``--steps`` timed sweeps run at D=4000 in the
+split form (3xTF32 matvec on the tensor cores, FP64-accurate environments
+and Rayleigh energies, FP64 Lanczos recurrence and SVD).
 
-* ``value``: seconds per sweep at D=2000, device-resident state, CUDA events
+* ``value``: seconds per sweep at D=4000, device-resident state, CUDA events
   on the library's stream around the timed sweeps (lower is better).  The
   state (several GB) is far larger than L2, so no flush is needed.
-* ``e2e``: the same sweep through the C ABI from host buffers: upload of the
-  MPS, MPO and right environments, the sweep, download of the MPS and right
-  environments -- the drop-in call's work.
-* ``roofline``, ``kernels``, ``gpu_launches``: from one more sweep at D=2000
-  run under the library's kernel profiler (CUDA events around every kernel
+* ``fp64``: ``--fp64-sweeps`` sweeps of the same state in the plain FP64 form
+  (FP64 FMA end to end), timed the same way; ``split_speedup`` = FP64 sweep
+  time / split sweep time, with both forms' energies and |dE/E| between them.
+* ``e2e``: the same split sweep through the C ABI from host buffers: upload
+  of the MPS, MPO and right environments, the sweep, download of the MPS
+  and right environments -- the drop-in call's work.
+* ``roofline``, ``kernels``, ``gpu_launches``: from one more split sweep run
+  under the library's kernel profiler (CUDA events around every kernel
   family on the library stream; the Lanczos matvec then runs launch by
   launch instead of as a replayed CUDA graph): the kernel family with the
   most device time, its algorithmic flops (2*m*n*k over the QN-allowed
   block products) or bytes / its event time, against the measured peak.
-* ``cpu_baseline``: the FP64 CPU restatement (numpy + the host BLAS) on one
-  central two-site update of the same state, scaled to a sweep by the GPU's
-  own ratio of sweep time to that update's time.
-* ``--impl reference``: the same CPU restatement on the same kind of central
-  update (block structure recorded from a GPU run), the reference's own
-  gqten+MKL path being unbuildable here.
+* ``cpu_baseline``: the FP64 CPU restatement (numpy + the host BLAS, all
+  host threads) on real two-site updates of the same state at bonds spread
+  evenly over the chain; a sweep is estimated as 2(L-1) times their mean
+  update time.  Its energy at the centre bond is compared with the GPU's.
+* ``--impl reference``: the same CPU restatement on the same kind of updates
+  (block structures at eight evenly spaced bonds recorded from a GPU run of
+  this workload, ``--record-structure``; random data; Lanczos capped at the
+  recorded iteration counts), the reference's own gqten+MKL path being
+  unbuildable here; the same sweep estimate.
 
-Other workloads (not the headline line): ``--model hubbard`` (L=64 Fermi-
-Hubbard chain, t=1, U=8, half filling, D 1000 -> 4000 over 8 sweeps) and
+Other workloads (not the headline line): ``--model heisenberg`` (L=100
+chain, D 500 -> 2000), ``--model j1j2`` (4x16 cylinder, D 2000 -> 6000) and
 ``--workload batched`` (64 seeded XXZ chains, L in [16, 64], Delta in
 [0.5, 1.5], D in {64..512}, 4 sweeps each, run concurrently and one after
 another; the metric is instances per second).
@@ -49,34 +58,56 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SCHEDULE = [500, 800, 1100, 1400, 1700, 2000]
-L_SITES = 100
+MODELS = {
+    "hubbard": {"L": 64, "schedule": [1000, 1430, 1860, 2290, 2710, 3140, 3570, 4000],
+                "workload": "hubbard_obc_L64_U8_half_filling_D1000to4000"},
+    "heisenberg": {"L": 100, "schedule": [500, 800, 1100, 1400, 1700, 2000],
+                   "workload": "heisenberg_obc_L100_Sz0_D500to2000"},
+    "j1j2": {"L": 64, "Lx": 16, "Ly": 4, "J1": 1.0, "J2": 0.5,
+             "schedule": [2000, 2570, 3140, 3710, 4290, 4860, 5430, 6000],
+             "workload": "j1j2_cylinder_4x16_snake_J2_0.5_D2000to6000"},
+}
+L_SITES = MODELS["hubbard"]["L"]
+WORKLOAD = MODELS["hubbard"]["workload"]
+SCHEDULE = MODELS["hubbard"]["schedule"]
 LANCZOS = (1e-10, 100)
-WORKLOAD = "heisenberg_obc_L100_Sz0_D500to2000"
 FAMILIES = ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc", "permute", "vector", "skinny")
-STRUCTURE_FIXTURE = os.path.join(ROOT, "tests", "golden", "bench_center_bond.json")
+N_BONDS = 8   # bonds of the CPU sweep estimate, evenly spaced over the chain
+
+
+def _structure_fixture(model):
+    return os.path.join(ROOT, "tests", "golden", f"bench_bonds_{model}.json")
+
+
+def _sample_bonds(L, n=N_BONDS):
+    """n 'r'-update sites evenly spaced over the L-1 bonds (each stands for
+    (L-1)/n of them); a sweep's 2(L-1) updates are estimated as 2(L-1)
+    times the mean update time at these sites."""
+    return [min(L - 3, max(1, int(round((k + 0.5) * (L - 1) / n)))) for k in range(n)]
 
 
 def _args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", choices=["fp64", "tf32x3", "fp64tc"], default="tf32x3")
     p.add_argument("--rayleigh", choices=["fp64", "fp64tc"], default="fp64tc",
                    help="arithmetic of the split form's Rayleigh-quotient energies")
-    p.add_argument("--model", choices=["heisenberg", "hubbard", "j1j2"], default="heisenberg",
-                   help="heisenberg: L=100 chain, D 500->2000 (headline); hubbard: L=64 "
-                        "chain, U=8, half filling, D 1000->4000; j1j2: 4x16 open cylinder "
+    p.add_argument("--model", choices=sorted(MODELS), default="hubbard",
+                   help="hubbard: L=64 chain, U=8, half filling, D 1000->4000 (headline); "
+                        "heisenberg: L=100 chain, D 500->2000; j1j2: 4x16 open cylinder "
                         "(snake order), J1=1, J2=0.5, D 2000->6000")
     p.add_argument("--schedule", default=None,
                    help="comma-separated D per growth sweep; the last is the timed D")
+    p.add_argument("--fp64-sweeps", type=int, default=1,
+                   help="timed sweeps of the plain FP64 form after the split ones")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--record-structure", action="store_true",
-                   help="write the central-bond block structure fixture")
+                   help="write the block structures of the sampled bonds (reference arm)")
     p.add_argument("--workload", choices=["sweep", "batched"], default="sweep",
-                   help="sweep: the D=2000 chain (headline); batched: 64 independent XXZ "
+                   help="sweep: the chain of --model; batched: 64 independent XXZ "
                         "chains, concurrent vs one after another")
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--threads", type=int, default=16)
@@ -169,41 +200,35 @@ def _fp64_peak_tflops(torch):
     return best
 
 
-HUBBARD = {"L": 64, "schedule": [1000, 1430, 1860, 2290, 2710, 3140, 3570, 4000],
-           "workload": "hubbard_obc_L64_U8_half_filling_D1000to4000"}
-J1J2 = {"L": 64, "Lx": 16, "Ly": 4, "J1": 1.0, "J2": 0.5,
-        "schedule": [2000, 2570, 3140, 3710, 4290, 4860, 5430, 6000],
-        "workload": "j1j2_cylinder_4x16_snake_J2_0.5_D2000to6000"}
-
-
 def _select_model(args):
-    """Module constants for the chosen model (heisenberg: the headline chain;
-    hubbard: L=64, t=1, U=8, half filling, Sz=0, U(1)xU(1), Jordan-Wigner
-    MPO of bond dimension 6, alternating up/down product state; j1j2: the
-    4x16 open cylinder in snake order, J1=1, J2=0.5, Sz=0, shuffled Neel
-    product state, MPO from the generator's compression, bond dimension <= 17)."""
+    """Module constants for the chosen model (hubbard: the headline chain,
+    L=64, t=1, U=8, half filling, Sz=0, U(1)xU(1), Jordan-Wigner MPO of bond
+    dimension 6, alternating up/down product state; heisenberg: the L=100
+    chain, shuffled Neel product state; j1j2: the 4x16 open cylinder in snake
+    order, J1=1, J2=0.5, Sz=0, shuffled Neel product state, MPO from the
+    generator's compression, bond dimension <= 17)."""
     global L_SITES, WORKLOAD, SCHEDULE
-    if args.model == "hubbard":
-        L_SITES, WORKLOAD, SCHEDULE = HUBBARD["L"], HUBBARD["workload"], HUBBARD["schedule"]
-    elif args.model == "j1j2":
-        L_SITES, WORKLOAD, SCHEDULE = J1J2["L"], J1J2["workload"], J1J2["schedule"]
+    m = MODELS[args.model]
+    L_SITES, WORKLOAD, SCHEDULE = m["L"], m["workload"], m["schedule"]
     if args.schedule is None:
         args.schedule = ",".join(map(str, SCHEDULE))
 
 
-def _model(model="heisenberg"):
+def _model(model="hubbard"):
     from mps2_gb300 import hamiltonians as H
     from mps2_gb300.finite_mps import DirectStateInitMps, FiniteMPS
+    L = MODELS[model]["L"]
     if model == "hubbard":
-        sv, mpo, qn0, gen = H.hubbard_chain(L_SITES, 1.0, 8.0)
-        labels = [1 if i % 2 == 0 else 2 for i in range(L_SITES)]
+        sv, mpo, qn0, gen = H.hubbard_chain(L, 1.0, 8.0)
+        labels = [1 if i % 2 == 0 else 2 for i in range(L)]
     elif model == "j1j2":
-        pairs = H.j1j2_cylinder_pairs(J1J2["Lx"], J1J2["Ly"], J1J2["J1"], J1J2["J2"])
-        sv, mpo, qn0, gen = H.heisenberg_pairs(L_SITES, pairs)
-        labels = H.neel_shuffled_labels(L_SITES, 0)
+        m = MODELS["j1j2"]
+        pairs = H.j1j2_cylinder_pairs(m["Lx"], m["Ly"], m["J1"], m["J2"])
+        sv, mpo, qn0, gen = H.heisenberg_pairs(L, pairs)
+        labels = H.neel_shuffled_labels(L, 0)
     else:
-        sv, mpo, qn0, gen = H.heisenberg_chain(L_SITES)
-        labels = H.neel_shuffled_labels(L_SITES, 0)
+        sv, mpo, qn0, gen = H.heisenberg_chain(L)
+        labels = H.neel_shuffled_labels(L, 0)
     mps = FiniteMPS(sv)
     DirectStateInitMps(mps, labels, qn0)
     return mps, mpo
@@ -216,11 +241,13 @@ def _tensor_bytes(t):
 # ---------------------------------------------------------------------------
 # CPU restatement timing (oracle) -- test infrastructure used as the baseline
 # ---------------------------------------------------------------------------
-def _oracle_center_update(mpsd, mpo, envs, c, D, iters_cap=None):
-    """Time one 'r' two-site update at site c with the FP64 CPU restatement.
-    mpsd: {site: tensor}, envs: {('l'|'r', len): tensor} (product tensors)."""
+def _oracle_update(mpsd, mpo, envs, c, D, iters_cap=None):
+    """Time one 'r' two-site update at site c with the FP64 CPU restatement
+    (the oracle).  mpsd: {site: tensor}, envs: {('l'|'r', len): tensor}
+    (product tensors); iters_cap: Lanczos iterations at most (the GPU's
+    count for this update)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle
+    import oracle  # noqa: F401
     from oracle.lanczos import LanczosParams as OLP
     from oracle.vmps import SweepParams as OSP, two_site_update
     from _convert import to_oracle
@@ -236,82 +263,94 @@ def _oracle_center_update(mpsd, mpo, envs, c, D, iters_cap=None):
     return time.perf_counter() - t0, st
 
 
-def _synthetic_center_state(fix, seed=0):
-    """Random tensors with the recorded central-bond block structure."""
+def _describe_index(ix):
+    return {"dir": ix.dir, "sectors": [[list(q), d] for q, d in ix.sectors()]}
+
+
+def _synthetic_bond(model, L, rec, seed):
+    """Random tensors with a recorded bond's block structure."""
     import numpy as np
-    from mps2_gb300.hamiltonians import heisenberg_chain
     from mps2_gb300.tensor import GQTensor, Index
     rng = np.random.default_rng(seed)
-    N = fix["L"]
-    c = fix["center"]
-    sv, mpo, qn0, _ = heisenberg_chain(N)
+    c = rec["site"]
+    _, mpo = _model(model)
 
     def idx(d):
         return Index([(tuple(q), n) for q, n in d["sectors"]], d["dir"])
 
     def rand(indices, div):
-        t = GQTensor(indices, div)
-        for cc in t.allowed_coords(div):
+        t = GQTensor(indices, tuple(div))
+        for cc in t.allowed_coords(tuple(div)):
             t.blocks[cc] = rng.standard_normal(t.block_shape(cc))
         return t
 
-    A = rand([idx(d) for d in fix["A_c"]], (0,))
-    B = rand([idx(d) for d in fix["A_c1"]], (0,))
-    Le = rand([idx(d) for d in fix["L"+"_env"]], (0,))
-    Re = rand([idx(d) for d in fix["R_env"]], (0,))
-    return {c: A, c + 1: B}, mpo, {("l", c): Le, ("r", N - c - 2): Re}
+    A = rand([idx(d) for d in rec["A_c"]], rec["div_c"])
+    B = rand([idx(d) for d in rec["A_c1"]], rec["div_c1"])
+    Le = rand([idx(d) for d in rec["L_env"]], rec["div_l"])
+    Re = rand([idx(d) for d in rec["R_env"]], rec["div_r"])
+    return {c: A, c + 1: B}, mpo, {("l", c): Le, ("r", L - c - 2): Re}
 
 
-def _describe_index(ix):
-    return {"dir": ix.dir, "sectors": [[list(q), d] for q, d in ix.sectors()]}
+def _cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
 
 
 # ---------------------------------------------------------------------------
 def run_reference(args):
-    """CPU restatement on a central update with the recorded structure."""
+    """CPU restatement on two-site updates with the recorded block
+    structures of evenly spaced bonds, one bond per step (cycling)."""
     ws, rank = _dist()
     if rank != 0:
         return
-    if args.model != "heisenberg":
+    path = _structure_fixture(args.model)
+    if not os.path.exists(path):
         print(json.dumps({"impl": "reference",
-                          "unavailable": "the recorded central-bond structure is the "
-                                         "Heisenberg chain's only"}))
+                          "unavailable": f"no recorded bond structures for the {args.model} "
+                                         "workload (bench.py --record-structure)"}))
         return
-    if not os.path.exists(STRUCTURE_FIXTURE):
-        print(json.dumps({"impl": "reference",
-                          "unavailable": "central-bond structure fixture missing"}))
-        return
-    with open(STRUCTURE_FIXTURE) as f:
+    with open(path) as f:
         fix = json.load(f)
-    D = fix["D"]
-    c = fix["center"]
-    mpsd, mpo, envs = _synthetic_center_state(fix)
-    times = []
-    for _ in range(args.warmup):
-        _oracle_center_update(dict(mpsd), mpo, dict(envs), c, D, fix["center_iters"])
-    for _ in range(max(1, args.steps)):
-        t, st = _oracle_center_update(dict(mpsd), mpo, dict(envs), c, D, fix["center_iters"])
-        times.append(t)
-    per_update = sum(times) / len(times)
-    sweep_s = per_update * fix["sweep_over_center"]
-    cores = os.cpu_count()
+    D, L, recs = fix["D"], fix["L"], fix["bonds"]
+    # untimed warm-up steps on the cheapest recorded bond
+    cheap = min(recs, key=lambda r: r["theta_size"])
+    for w in range(args.warmup):
+        mpsd, mpo, envs = _synthetic_bond(args.model, L, cheap, 1000 + w)
+        _oracle_update(mpsd, mpo, envs, cheap["site"], D, cheap["iters"])
+    per_bond = {}
+    for k in range(max(1, args.steps)):
+        rec = recs[k % len(recs)]
+        mpsd, mpo, envs = _synthetic_bond(args.model, L, rec, k)
+        t, _ = _oracle_update(mpsd, mpo, envs, rec["site"], D, rec["iters"])
+        per_bond.setdefault(rec["site"], []).append(t)
+    means = [sum(v) / len(v) for v in per_bond.values()]
+    per_update = sum(means) / len(means)
+    sweep_s = per_update * 2 * (L - 1)
+    sample = (f"{args.steps} two-site update(s), one per step, cycling over {len(per_bond)} of "
+              f"the {len(recs)} recorded bonds (sites {sorted(per_bond)}), D={D}, random data "
+              f"with the recorded block structures, Lanczos capped at the recorded iteration "
+              f"counts; sweep = 2(L-1) x mean over bonds of the mean update time")
     line = {
         "metric": f"DMRG sweep time (s/sweep) at D={D}",
         "value": sweep_s, "unit": "s/sweep", "impl": "reference", "n_gpus": args.gpus,
-        "steps": len(times), "warmup": args.warmup, "ms_per_step": per_update * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_update * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (random tensors with the central-bond block structure recorded "
-                "from a GPU run of this workload)",
-        "config": {"workload": WORKLOAD, "D": D, "L": fix["L"],
-                   "cache": "inputs larger than L2"},
-        "cpu_baseline": {"value": sweep_s, "unit": "s/sweep", "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} central two-site update(s) at site {c}, "
-                                   f"D={D}, Lanczos capped at {fix['center_iters']} iterations, "
-                                   f"x{fix['sweep_over_center']:.1f} (GPU sweep/update time ratio)"},
+        "data": "synthetic (random tensors with block structures recorded from a GPU run of "
+                "this workload)",
+        "config": {"workload": WORKLOAD, "D": D, "L": L, "cache": "inputs larger than L2"},
+        "per_bond_seconds": {str(k): v for k, v in sorted(per_bond.items())},
+        "cpu_baseline": {"value": sweep_s, "unit": "s/sweep", "cores": _cpu_threads(),
+                         "kind": "port", "sample": sample},
         "e2e": {"value": sweep_s, "unit": "s/sweep", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def _stats_sum(stats, key):
+    return sum(getattr(s, key) for s in stats)
 
 
 def run_ours(args):
@@ -337,18 +376,34 @@ def run_ours(args):
     st = DMRGState(mps.tens, mpo)
     t_setup = time.perf_counter()
     st.init_envs(args.precision)
-    for d in sched[:-1]:
+    for d in sched:
         e0, stats = st.sweep(params(d))
         print(f"[setup] sweep at D={d}: E0={e0:.12f} max bond {max(x.D for x in stats)} "
-              f"({sum(x.update_seconds for x in stats):.1f}s)", file=sys.stderr)
+              f"({_stats_sum(stats, 'update_seconds'):.1f}s)", file=sys.stderr)
     for w in range(args.warmup):
         e0, stats = st.sweep(params(D))
-        print(f"[warmup {w}] D={D} E0={e0:.12f} {sum(x.update_seconds for x in stats):.1f}s",
+        print(f"[warmup {w}] D={D} E0={e0:.12f} {_stats_sum(stats, 'update_seconds'):.1f}s",
               file=sys.stderr)
     setup_s = time.perf_counter() - t_setup
 
-    # ---- timed sweeps -------------------------------------------------------
     ext = torch.cuda.ExternalStream(library_stream())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    def timed_sweeps(n, prec):
+        """n sweeps at D timed with CUDA events on the library stream."""
+        out_stats, energies = [], []
+        torch.cuda.synchronize()
+        ev0.record(ext)
+        for _ in range(n):
+            e, s_ = st.sweep(params(D, prec))
+            out_stats.extend(s_)
+            energies.append(e)
+        ev1.record(ext)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) * 1e-3, out_stats, energies
+
+    # ---- timed sweeps (split form, the headline) ------------------------------
     clocks = ClockSampler(local)
     if ws > 1:
         dist.barrier()
@@ -357,29 +412,33 @@ def run_ours(args):
     # an external profiler started with --profile-from-start off records the
     # timed sweeps only
     torch.cuda.profiler.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(ext)
-    timed_stats, energies = [], []
-    for k in range(args.steps):
-        e0, stats = st.sweep(params(D))
-        timed_stats.extend(stats)
-        energies.append(e0)
-    ev1.record(ext)
-    torch.cuda.synchronize()
+    t_split, timed_stats, energies = timed_sweeps(args.steps, args.precision)
     torch.cuda.profiler.stop()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
+    ms = t_split * 1e3
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     sweep_s = ms * 1e-3 / args.steps
 
-    # ---- one more sweep under the kernel profiler (CUDA events around every
-    # kernel family; the Lanczos matvec then runs without graph replay): the
-    # kernel shares, launch count and roofline come from it -------------------
+    # ---- the plain FP64 form on the same state, timed the same way -----------
+    fp64 = None
+    if args.fp64_sweeps > 0 and args.precision != "fp64":
+        t64, st64, e64 = timed_sweeps(args.fp64_sweeps, "fp64")
+        s64 = t64 / args.fp64_sweeps
+        fp64 = {"sweep_s": s64, "sweeps": args.fp64_sweeps, "energies": e64,
+                "split_speedup": s64 / sweep_s,
+                "delta_e_rel_split_vs_fp64": abs(energies[-1] - e64[-1]) / abs(e64[-1]),
+                "time_split_s": {"lanczos": _stats_sum(st64, "lanczos_seconds"),
+                                 "svd": _stats_sum(st64, "svd_seconds"),
+                                 "env": _stats_sum(st64, "env_seconds")},
+                "matvec_tflops": _stats_sum(st64, "matvec_flops") /
+                max(_stats_sum(st64, "lanczos_seconds"), 1e-9) / 1e12}
+
+    # ---- one more split sweep under the kernel profiler ------------------------
     profile_enable(True)
+    torch.cuda.synchronize()
     ev0.record(ext)
     st.sweep(params(D))
     ev1.record(ext)
@@ -387,7 +446,7 @@ def run_ours(args):
     prof_sweep_s = ev0.elapsed_time(ev1) * 1e-3
     prof = {k: profile_read(k) for k in FAMILIES}
     svd_span = {k: profile_read(k) for k in ("svd", "svd_eig", "svd_gather", "svd_factors",
-                                              "svd_ortho")}
+                                              "svd_ortho", "svd_gram", "svd_reduce")}
     profile_enable(False)
     n_launch_ours = sum(v[0] for v in prof.values())
 
@@ -407,55 +466,81 @@ def run_ours(args):
     out_env = [st2.get_env("r", n) for n in range(1, L_SITES - 1)]
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    del st2, out_mps, out_env
+    del st2, out_mps, out_env, host_mps, host_renv
 
-    # ---- the central two-site problem: FP64 vs split, CPU restatement ------
-    c = L_SITES // 2 - 1
-    for i in range(0, c):
-        st.update(params(D), "r", i)
-    mpsd = {c: st.get_mps(c), c + 1: st.get_mps(c + 1)}
-    envs = {("l", c): st.get_env("l", c), ("r", L_SITES - c - 2): st.get_env("r", L_SITES - c - 2)}
-    theta = Contract(mpsd[c], mpsd[c + 1], ([2], [0]))
-    eff = [envs[("l", c)], mpo[c], mpo[c + 1], envs[("r", L_SITES - c - 2)]]
-    solve = {}
-    for prec in ("fp64", "tf32x3", "fp64tc"):
-        profile_enable(True)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = LanczosSolver(eff, theta, lp, "cent", precision=prec, rayleigh=args.rayleigh)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        pr = {k: profile_read(k) for k in FAMILIES}
-        profile_enable(False)
-        gemm_ms = sum(pr[k][1] for k in ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc", "skinny"))
-        gemm_fl = sum(pr[k][2] for k in ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc", "skinny"))
-        solve[prec] = {"energy": r.gs_eng, "iters": r.iters, "seconds": dt,
-                       "kernel_ms": {k: pr[k][1] for k in FAMILIES},
-                       "matvec_gemm_tflops": gemm_fl / (gemm_ms * 1e-3) / 1e12 if gemm_ms else None,
-                       "tc_gemm_tflops": (pr["gemm_tf32x3"][2] / (pr["gemm_tf32x3"][1] * 1e-3) / 1e12
-                                          if pr["gemm_tf32x3"][1] else None)}
-    de = abs(solve["tf32x3"]["energy"] - solve["fp64"]["energy"]) / abs(solve["fp64"]["energy"])
-    gpu_center = st.update(params(D), "r", c)
+    # ---- bonds of the CPU estimate: a half sweep to the right, stopping at
+    # the sampled sites (the state is converged, so this only moves the
+    # centre); at the centre bond the Lanczos problem in all three forms ------
+    bonds = _sample_bonds(L_SITES)
+    centre = bonds[len(bonds) // 2]
+    recs, cpu_times, solve, gpu_centre, cpu_centre = [], {}, {}, None, None
+    cpu_bonds = [] if (rank != 0 or args.no_cpu_baseline) else [bonds[1], centre, bonds[-2]]
+    i = 0
+    for b in bonds:
+        while i < b:
+            st.update(params(D), "r", i)
+            i += 1
+        mpsd = {b: st.get_mps(b), b + 1: st.get_mps(b + 1)}
+        envs = {("l", b): st.get_env("l", b),
+                ("r", L_SITES - b - 2): st.get_env("r", L_SITES - b - 2)}
+        if b == centre:
+            theta = Contract(mpsd[b], mpsd[b + 1], ([2], [0]))
+            eff = [envs[("l", b)], mpo[b], mpo[b + 1], envs[("r", L_SITES - b - 2)]]
+            for prec in ("fp64", "tf32x3", "fp64tc"):
+                profile_enable(True)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                r = LanczosSolver(eff, theta, lp, "cent", precision=prec, rayleigh=args.rayleigh)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t0
+                pr = {k: profile_read(k) for k in FAMILIES}
+                profile_enable(False)
+                gemm = ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc", "skinny")
+                gemm_ms = sum(pr[k][1] for k in gemm)
+                gemm_fl = sum(pr[k][2] for k in gemm)
+                solve[prec] = {"energy": r.gs_eng, "iters": r.iters, "seconds": dt,
+                               "kernel_ms": {k: pr[k][1] for k in FAMILIES},
+                               "matvec_gemm_tflops": gemm_fl / (gemm_ms * 1e-3) / 1e12
+                               if gemm_ms else None}
+        g = st.update(params(D), "r", b)
+        i = b + 1
+        if b == centre:
+            gpu_centre = g
+        if args.record_structure and rank == 0:
+            recs.append({
+                "site": b, "iters": int(max(1, g.iters)), "theta_size": int(g.theta_size),
+                "A_c": [_describe_index(ix) for ix in mpsd[b].indices],
+                "A_c1": [_describe_index(ix) for ix in mpsd[b + 1].indices],
+                "L_env": [_describe_index(ix) for ix in envs[("l", b)].indices],
+                "R_env": [_describe_index(ix) for ix in envs[("r", L_SITES - b - 2)].indices],
+                "div_c": list(mpsd[b].div), "div_c1": list(mpsd[b + 1].div),
+                "div_l": list(envs[("l", b)].div),
+                "div_r": list(envs[("r", L_SITES - b - 2)].div)})
+        if b in cpu_bonds:
+            t_cpu, ost = _oracle_update(mpsd, mpo, envs, b, D, int(max(1, g.iters)))
+            cpu_times[b] = t_cpu
+            if b == centre:
+                cpu_centre = ost
+        del mpsd, envs
     if args.record_structure and rank == 0:
-        center_struct = {
-            "L": L_SITES, "center": c, "D": D, "center_iters": int(max(1, gpu_center.iters)),
-            "sweep_over_center": sweep_s / gpu_center.update_seconds,
-            "A_c": [_describe_index(ix) for ix in mpsd[c].indices],
-            "A_c1": [_describe_index(ix) for ix in mpsd[c + 1].indices],
-            "L_env": [_describe_index(ix) for ix in envs[("l", c)].indices],
-            "R_env": [_describe_index(ix) for ix in envs[("r", L_SITES - c - 2)].indices],
-        }
-        os.makedirs(os.path.dirname(STRUCTURE_FIXTURE), exist_ok=True)
-        with open(STRUCTURE_FIXTURE, "w") as f:
-            json.dump(center_struct, f)
+        path = _structure_fixture(args.model)
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            json.dump({"L": L_SITES, "D": D, "model": args.model, "bonds": recs}, f)
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        t_cpu, ost = _oracle_center_update(mpsd, mpo, envs, c, D)
-        cpu = {"value": sweep_s * t_cpu / gpu_center.update_seconds, "unit": "s/sweep",
-               "cores": os.cpu_count(), "kind": "port",
-               "sample": (f"1 central two-site update (site {c}, D={D}) of the same state: CPU "
-                          f"{t_cpu:.2f}s vs GPU {gpu_center.update_seconds:.3f}s, scaled by the "
-                          f"GPU sweep time; CPU E0={ost.e0:.12f} GPU E0={gpu_center.e0:.12f}")}
+    if cpu_times:
+        mean_t = sum(cpu_times.values()) / len(cpu_times)
+        cpu = {"value": mean_t * 2 * (L_SITES - 1), "unit": "s/sweep", "cores": _cpu_threads(),
+               "kind": "port",
+               "sample": (f"{len(cpu_times)} two-site updates of this run's converged D={D} "
+                          f"state at sites {sorted(cpu_times)} (CPU seconds "
+                          f"{[round(cpu_times[k], 2) for k in sorted(cpu_times)]}), Lanczos "
+                          f"capped at the GPU's iteration count; sweep = 2(L-1) x mean "
+                          f"update time"),
+               "centre_energy_cpu": cpu_centre.e0 if cpu_centre else None,
+               "centre_energy_gpu": gpu_centre.e0 if gpu_centre else None}
+        if cpu_centre is not None and gpu_centre is not None:
+            cpu["centre_delta_e_rel"] = abs(gpu_centre.e0 - cpu_centre.e0) / abs(cpu_centre.e0)
 
     # ---- roofline of the dominant kernel family ------------------------------
     peaks, peak_kind = _measured_peaks()
@@ -475,39 +560,43 @@ def run_ours(args):
     achieved = ((fl / 1e12) if unit == "TFLOP/s" else (by / 1e9)) / (t_ms * 1e-3) if t_ms else 0.0
     kernels = {k: {"launches": v[0], "ms": v[1],
                    "share_of_sweep": v[1] * 1e-3 / prof_sweep_s} for k, v in prof.items()}
-    tot = {k: sum(getattr(s, k) for s in timed_stats) for k in
-           ("lanczos_seconds", "svd_seconds", "env_seconds", "update_seconds", "matvec_flops",
-            "env_flops", "matvecs")}
-    u64 = gpu_center.update_seconds - gpu_center.lanczos_seconds + solve["fp64"]["seconds"]
+    for k in ("vector", "skinny", "permute"):
+        n_k, ms_k, _, by_k = prof[k]
+        kernels[k]["gbs"] = by_k / 1e9 / (ms_k * 1e-3) if ms_k else None
+    for k in ("gemm_fp64", "gemm_tf32x3", "gemm_fp64tc"):
+        n_k, ms_k, fl_k, _ = prof[k]
+        kernels[k]["tflops"] = fl_k / 1e12 / (ms_k * 1e-3) if ms_k else None
     line = {
         "metric": f"DMRG sweep time (s/sweep) at D={D}",
         "value": sweep_s, "unit": "s/sweep", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sweep_s * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "tf32x3 split products, f64 sums",
-        "data": "synthetic model (Heisenberg chain), no dataset",
+        "dtype": "f64" if args.precision == "fp64" else f"{args.precision} split products, f64 sums",
+        "data": f"synthetic model ({args.model}), no dataset",
         "config": {"workload": WORKLOAD, "L": L_SITES, "D": D, "schedule": sched,
-                   "precision": args.precision, "lanczos": list(LANCZOS),
-                   "parallelism": f"replicas x{ws}", "cache": "inputs larger than L2",
-                   "setup_seconds": setup_s},
+                   "precision": args.precision, "rayleigh": args.rayleigh,
+                   "lanczos": list(LANCZOS), "parallelism": f"replicas x{ws}",
+                   "cache": "inputs larger than L2", "setup_seconds": setup_s},
         "energy_last_sweep": energies[-1],
+        "energies": energies,
+        "fp64": fp64,
         "gpu_launches": int(n_launch_ours),
         "profiled_sweep_s": prof_sweep_s,
-        "time_split_s": {"lanczos": tot["lanczos_seconds"], "svd": tot["svd_seconds"],
-                         "env": tot["env_seconds"], "matvecs": tot["matvecs"],
+        "time_split_s": {"lanczos": _stats_sum(timed_stats, "lanczos_seconds"),
+                         "svd": _stats_sum(timed_stats, "svd_seconds"),
+                         "env": _stats_sum(timed_stats, "env_seconds"),
+                         "matvecs": _stats_sum(timed_stats, "matvecs"),
                          "svd_device_span": svd_span["svd"][1] * 1e-3,
                          "svd_decompositions": svd_span["svd_eig"][1] * 1e-3,
+                         "svd_gram": svd_span["svd_gram"][1] * 1e-3,
+                         "svd_reduction": svd_span["svd_reduce"][1] * 1e-3,
                          "svd_gather": svd_span["svd_gather"][1] * 1e-3,
                          "svd_factors": svd_span["svd_factors"][1] * 1e-3,
-                         "svd_ortho": svd_span["svd_ortho"][1] * 1e-3,
-                         "svd_ortho_calls": svd_span["svd_ortho"][0]},
-        "central_problem": {"fp64": solve["fp64"], "tf32x3": solve["tf32x3"],
-                            "fp64tc": solve["fp64tc"],
-                            "delta_e_rel": de,
-                            "delta_e_rel_fp64tc": abs(solve["fp64tc"]["energy"] -
-                                                      solve["fp64"]["energy"]) /
-                            abs(solve["fp64"]["energy"]),
-                            "fp64_sweep_s_est": sweep_s * u64 / gpu_center.update_seconds},
+                         "svd_completion_qr": svd_span["svd_ortho"][1] * 1e-3},
+        "centre_problem": dict(solve, **({"delta_e_rel_split": abs(
+            solve["tf32x3"]["energy"] - solve["fp64"]["energy"]) / abs(solve["fp64"]["energy"]),
+            "delta_e_rel_fp64tc": abs(solve["fp64tc"]["energy"] - solve["fp64"]["energy"]) /
+            abs(solve["fp64"]["energy"])} if solve else {})),
         "kernels": kernels,
         "roofline": {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak,
                      "unit": unit, "frac": achieved / peak if peak else None, "traffic": None,
