@@ -447,6 +447,7 @@ def run_ours(args):
     prof = {k: profile_read(k) for k in FAMILIES}
     svd_span = {k: profile_read(k) for k in ("svd", "svd_eig", "svd_gather", "svd_factors",
                                               "svd_ortho", "svd_gram", "svd_reduce")}
+    host_plan = profile_read("host_plan")
     profile_enable(False)
     n_launch_ours = sum(v[0] for v in prof.values())
 
@@ -592,7 +593,9 @@ def run_ours(args):
                          "svd_reduction": svd_span["svd_reduce"][1] * 1e-3,
                          "svd_gather": svd_span["svd_gather"][1] * 1e-3,
                          "svd_factors": svd_span["svd_factors"][1] * 1e-3,
-                         "svd_completion_qr": svd_span["svd_ortho"][1] * 1e-3},
+                         "svd_completion_qr": svd_span["svd_ortho"][1] * 1e-3,
+                         "host_planning": host_plan[1] * 1e-3,
+                         "host_plans": host_plan[0]},
         "centre_problem": dict(solve, **({"delta_e_rel_split": abs(
             solve["tf32x3"]["energy"] - solve["fp64"]["energy"]) / abs(solve["fp64"]["energy"]),
             "delta_e_rel_fp64tc": abs(solve["fp64tc"]["energy"] - solve["fp64"]["energy"]) /

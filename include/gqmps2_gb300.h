@@ -261,6 +261,9 @@ int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *para
 #define GQ_PROF_SVD_GRAM 11   /* of the decompositions: the Gram matrices */
 #define GQ_PROF_SVD_REDUCE 12 /* of the decompositions: their rank-revealing
                                  reduction, rank read-back included */
+#define GQ_PROF_HOST_PLAN 13  /* host wall time spent planning contractions
+                                 (work lists, kernel choice); "launches" counts
+                                 the plans */
 int gq_profile_enable(int on);
 /* Tile-choice autotuner (not in the reference): with `on`, every matvec
  * contraction whose block-size histogram has not been seen before times the

@@ -14,6 +14,7 @@
 // ordered (free, contracted) or (contracted, free); otherwise one batched
 // permute kernel reorders all of its blocks first.
 #include <array>
+#include <chrono>
 #include <map>
 #include <mutex>
 
@@ -100,6 +101,13 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
                                             const std::vector<int> &axes_b,
                                             const Tensor *target, Precision prec,
                                             double tc_frac) {
+  struct PlanTimer {  // host planning time, added to the profiler on every exit
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    ~PlanTimer() {
+      prof_host(kProfHostPlan,
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    }
+  } plan_timer;
   const int ra = a.rank(), rb = b.rank(), nc = (int)axes_a.size();
   GQ_CHECK(nc == (int)axes_b.size() && nc >= 1, "contraction needs matching, non-empty axes");
   GQ_CHECK(a.nq == b.nq, "operands use different charge counts");
@@ -725,7 +733,7 @@ void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, d
   else
     gemm_fp64_kernel<1, 1><<<grid, 256, 0, s>>>(p.tiles.p, p.pairs.p, A, B, C);
   GQ_CUDA(cudaGetLastError());
-  prof_end(kProfGemmFp64, p.flops - p.flops_tc, 8.0 * (double)(p.a_elems + p.b_elems));
+  prof_end(kProfGemmFp64, p.flops - p.flops_tc - p.flops_oz, 8.0 * (double)(p.a_elems + p.b_elems));
 }
 
 }  // namespace gq

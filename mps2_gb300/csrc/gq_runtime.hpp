@@ -84,12 +84,14 @@ enum ProfKernel : int {
   kProfSvdOrtho = 10,  // of which: QR of the null-space completions
   kProfSvdGram = 11,   // of the decompositions: the Gram matrices
   kProfSvdReduce = 12, // of the decompositions: rank-revealing reduction and rank read-back
-  kProfCount = 13,
+  kProfHostPlan = 13,  // host wall time of contraction planning (not device time)
+  kProfCount = 14,
 };
 bool prof_on();
 void prof_enable(bool on);
 void prof_begin(ProfKernel k);
 void prof_end(ProfKernel k, double flops, double bytes);
+void prof_host(ProfKernel k, double seconds);  // add host wall time to a counter
 void prof_read(ProfKernel k, int64_t *launches, double *ms, double *flops, double *bytes);
 
 // Arithmetic of the contractions (matvec, environment growth).

@@ -235,6 +235,12 @@ void prof_end(ProfKernel k, double flops, double bytes) {
   if (g_prof.pending.size() > 4096) prof_drain();
 }
 
+void prof_host(ProfKernel k, double seconds) {
+  if (!prof_on()) return;
+  g_prof.launches[k]++;
+  g_prof.ms[k] += seconds * 1e3;
+}
+
 void prof_read(ProfKernel k, int64_t *launches, double *ms, double *flops, double *bytes) {
   prof_drain();
   if (launches) *launches = g_prof.launches[k];

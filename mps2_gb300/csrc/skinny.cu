@@ -201,7 +201,7 @@ void launch_skinny(const ContractPlan &p, const double *A, const double *B, doub
   else
     skinny_kernel<32><<<grid, kSkRows, 0, s>>>(p.sk_items.p, p.sk_pairs.p, A, B, C);
   GQ_CUDA(cudaGetLastError());
-  prof_end(kProfSkinny, p.flops, 8.0 * (double)(p.a_elems + p.b_elems));
+  prof_end(kProfSkinny, p.flops, 8.0 * (double)(p.a_elems + p.b_elems + p.out->size()));
 }
 
 int skinny_rows_per_cta() { return kSkRows; }
