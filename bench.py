@@ -103,6 +103,8 @@ def _args():
                    help="comma-separated D per growth sweep; the last is the timed D")
     p.add_argument("--fp64-sweeps", type=int, default=1,
                    help="timed sweeps of the plain FP64 form after the split ones")
+    p.add_argument("--autotune", action="store_true",
+                   help="enable the tile-choice autotuner (gq_autotune_enable) for the run")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--record-structure", action="store_true",
                    help="write the block structures of the sampled bonds (reference arm)")
@@ -365,6 +367,9 @@ def run_ours(args):
     from mps2_gb300.vmps import (Contract, DMRGState, LanczosParams, LanczosSolver, SweepParams,
                                  library_stream, profile_enable, profile_read)
     _lib.check(_lib.load().gq_init(local))
+    if args.autotune:
+        from mps2_gb300.vmps import autotune_enable
+        autotune_enable(True)
     sched = [int(x) for x in args.schedule.split(",")]
     D = sched[-1]
     lp = LanczosParams(*LANCZOS)
@@ -576,7 +581,8 @@ def run_ours(args):
         "data": f"synthetic model ({args.model}), no dataset",
         "config": {"workload": WORKLOAD, "L": L_SITES, "D": D, "schedule": sched,
                    "precision": args.precision, "rayleigh": args.rayleigh,
-                   "lanczos": list(LANCZOS), "parallelism": f"replicas x{ws}",
+                   "lanczos": list(LANCZOS), "autotune": bool(args.autotune),
+                   "parallelism": f"replicas x{ws}",
                    "cache": "inputs larger than L2", "setup_seconds": setup_s},
         "energy_last_sweep": energies[-1],
         "energies": energies,

@@ -249,6 +249,19 @@ __global__ void shifted_identity_kernel(double *__restrict__ w, int dim, int k, 
   }
 }
 
+// dst = src with every zero written as +0.0.  A Householder reflector's
+// sign follows the sign of its pivot, and LAPACK reads the sign bit of an
+// exact zero pivot where the device QR takes it as positive: with signed
+// zeros removed the two agree.
+__global__ void plus_zero_copy_kernel(const double *__restrict__ src, double *__restrict__ dst,
+                                      int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = src[e];
+    dst[e] = v == 0.0 ? 0.0 : v;
+  }
+}
+
 template <typename T>
 void launch_items(void (*kern)(const T *, const double *, double *), const std::vector<T> &items,
                   const double *src, double *dst) {
@@ -299,7 +312,7 @@ void dense_contract_tc(const double *A, int64_t a0, int64_t a1, int axa, const d
 // factor of the complete Householder QR of `vecs` -- the unit vectors
 // e_r .. e_{r+k-1} carried through its r reflectors (geqrf, then ormqr on
 // the shifted identity; LAPACK's reflector conventions, as the oracle's
-// numpy QR).  O(dim r (r + k)) work, exactly orthonormal whatever the
+// numpy QR, on the vectors with signed zeros made +0.0).  O(dim r (r + k)) work, exactly orthonormal whatever the
 // overlap of the unit vectors with `vecs`.  The status words of the two
 // calls go to info_dev[0..1] (checked later by the caller).
 void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, double *out,
@@ -314,7 +327,9 @@ void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, doub
   auto sh = solver();
   const int d = (int)dim, kk = (int)k, rr = (int)r;
   DevBuf a(dim * r), tau(r);
-  GQ_CUDA(cudaMemcpyAsync(a.p, vecs, sizeof(double) * dim * r, cudaMemcpyDeviceToDevice, s));
+  plus_zero_copy_kernel<<<(unsigned)std::min<int64_t>((dim * r + 255) / 256, 4096), 256, 0, s>>>(
+      vecs, a.p, dim * r);
+  GQ_CUDA(cudaGetLastError());
   int lw1 = 0, lw2 = 0;
   GQ_SOLVER(cusolverDnDgeqrf_bufferSize(sh, d, rr, a.p, d, &lw1));
   GQ_SOLVER(cusolverDnDormqr_bufferSize(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, d, kk, rr, a.p, d,

@@ -372,13 +372,16 @@ def null_completion(q_nz: np.ndarray, dim: int, k: int, group: int = 0,
     through the r reflectors -- the basis states of the group that the
     nonzero vectors leave, made orthogonal to them.  O(dim r (r + k)) work;
     exactly orthonormal whatever the overlap of the unit vectors with
-    ``q_nz``.  With r = 0 it is the first k unit vectors.  (``group`` and
-    ``side`` do not enter.)"""
+    ``q_nz``.  With r = 0 it is the first k unit vectors.  Signed zeros of
+    ``q_nz`` are made +0.0 first: a reflector's sign follows its pivot's,
+    and an exact zero pivot counts as positive (LAPACK would read its sign
+    bit).  (``group`` and ``side`` do not enter.)"""
     if k == 0:
         return np.zeros((dim, 0))
     r = q_nz.shape[1]
     if r == 0:
         return np.eye(dim, k)
+    q_nz = np.where(q_nz == 0.0, 0.0, q_nz)
     qf = np.linalg.qr(q_nz, mode="complete")[0]
     return np.ascontiguousarray(qf[:, r:r + k])
 
