@@ -105,6 +105,9 @@ def _args():
                    help="timed sweeps of the plain FP64 form after the split ones")
     p.add_argument("--autotune", action="store_true",
                    help="enable the tile-choice autotuner (gq_autotune_enable) for the run")
+    p.add_argument("--profile-region", choices=["sweeps", "centre"], default="sweeps",
+                   help="what an external profiler started with --profile-from-start off "
+                        "records: the timed sweeps, or the centre bond's Lanczos solves")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--record-structure", action="store_true",
                    help="write the block structures of the sampled bonds (reference arm)")
@@ -415,10 +418,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     clocks.start()
     # an external profiler started with --profile-from-start off records the
-    # timed sweeps only
-    torch.cuda.profiler.start()
+    # timed sweeps only (or the centre bond's solves, below)
+    if args.profile_region == "sweeps":
+        torch.cuda.profiler.start()
     t_split, timed_stats, energies = timed_sweeps(args.steps, args.precision)
-    torch.cuda.profiler.stop()
+    if args.profile_region == "sweeps":
+        torch.cuda.profiler.stop()
     clk = clocks.stop()
     ms = t_split * 1e3
     if ws > 1:
@@ -453,6 +458,7 @@ def run_ours(args):
     svd_span = {k: profile_read(k) for k in ("svd", "svd_eig", "svd_gather", "svd_factors",
                                               "svd_ortho", "svd_gram", "svd_reduce")}
     host_plan = profile_read("host_plan")
+    host_sync = profile_read("host_sync")
     profile_enable(False)
     n_launch_ours = sum(v[0] for v in prof.values())
 
@@ -496,8 +502,12 @@ def run_ours(args):
                 profile_enable(True)
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
+                if args.profile_region == "centre":
+                    torch.cuda.profiler.start()
                 r = LanczosSolver(eff, theta, lp, "cent", precision=prec, rayleigh=args.rayleigh)
                 torch.cuda.synchronize()
+                if args.profile_region == "centre":
+                    torch.cuda.profiler.stop()
                 dt = time.perf_counter() - t0
                 pr = {k: profile_read(k) for k in FAMILIES}
                 profile_enable(False)
@@ -601,7 +611,9 @@ def run_ours(args):
                          "svd_factors": svd_span["svd_factors"][1] * 1e-3,
                          "svd_completion_qr": svd_span["svd_ortho"][1] * 1e-3,
                          "host_planning": host_plan[1] * 1e-3,
-                         "host_plans": host_plan[0]},
+                         "host_plans": host_plan[0],
+                         "host_sync_wait": host_sync[1] * 1e-3,
+                         "host_syncs": host_sync[0]},
         "centre_problem": dict(solve, **({"delta_e_rel_split": abs(
             solve["tf32x3"]["energy"] - solve["fp64"]["energy"]) / abs(solve["fp64"]["energy"]),
             "delta_e_rel_fp64tc": abs(solve["fp64tc"]["energy"] - solve["fp64"]["energy"]) /

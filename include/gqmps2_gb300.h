@@ -264,6 +264,9 @@ int gq_dmrg_run_batch(gq_dmrg *const *states, int n, const gq_sweep_params *para
 #define GQ_PROF_HOST_PLAN 13  /* host wall time spent planning contractions
                                  (work lists, kernel choice); "launches" counts
                                  the plans */
+#define GQ_PROF_HOST_SYNC 14  /* host wall time blocked waiting for the device
+                                 (stream synchronisations); "launches" counts
+                                 the waits */
 int gq_profile_enable(int on);
 /* Tile-choice autotuner (not in the reference): with `on`, every matvec
  * contraction whose block-size histogram has not been seen before times the

@@ -96,7 +96,7 @@ EXPORTS = {
 
 PROF = {"gemm_fp64": 0, "gemm_tf32x3": 1, "permute": 2, "vector": 3, "skinny": 4,
         "gemm_fp64tc": 5, "svd": 6, "svd_eig": 7, "svd_gather": 8, "svd_factors": 9,
-        "svd_ortho": 10, "svd_gram": 11, "svd_reduce": 12, "host_plan": 13}
+        "svd_ortho": 10, "svd_gram": 11, "svd_reduce": 12, "host_plan": 13, "host_sync": 14}
 
 _lib: Optional[C.CDLL] = None
 

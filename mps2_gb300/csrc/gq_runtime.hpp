@@ -85,7 +85,8 @@ enum ProfKernel : int {
   kProfSvdGram = 11,   // of the decompositions: the Gram matrices
   kProfSvdReduce = 12, // of the decompositions: rank-revealing reduction and rank read-back
   kProfHostPlan = 13,  // host wall time of contraction planning (not device time)
-  kProfCount = 14,
+  kProfHostSync = 14,  // host wall time blocked in stream synchronisations
+  kProfCount = 15,
 };
 bool prof_on();
 void prof_enable(bool on);

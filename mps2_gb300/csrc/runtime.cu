@@ -2,6 +2,7 @@
 #include "gq_runtime.hpp"
 
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -149,7 +150,16 @@ void upload_async(void *dst, const void *src, size_t bytes) {
   l.staging_head = off + bytes;
 }
 
-void sync() { GQ_CUDA(cudaStreamSynchronize(stream())); }
+void sync() {
+  if (!prof_on()) {
+    GQ_CUDA(cudaStreamSynchronize(stream()));
+    return;
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  GQ_CUDA(cudaStreamSynchronize(stream()));
+  prof_host(kProfHostSync,
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+}
 
 void DevBuf::alloc(int64_t elems) {
   release();
