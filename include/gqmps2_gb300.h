@@ -278,6 +278,12 @@ int gq_autotune_enable(int on);
 int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes);
 /* The cudaStream_t all library work is queued on. */
 int gq_get_stream(void **stream);
+/* Diagnostics (not in the reference): the number of times the library has
+ * waited on the host for its streams since it was loaded (every thread and
+ * lane).  A Lanczos solve on the main lane waits once; driven from the host
+ * (batched lanes, profiler on, GQ_NO_GRAPHS set) it waits once more per
+ * iteration. */
+int gq_host_sync_count(int64_t *count);
 
 #ifdef __cplusplus
 }

@@ -92,6 +92,7 @@ EXPORTS = {
     "gq_profile_enable": (_I, [_I]),
     "gq_profile_read": (_I, [_I, _I64P, _DP, _DP, _DP]),
     "gq_get_stream": (_I, [_PP]),
+    "gq_host_sync_count": (_I, [_I64P]),
 }
 
 PROF = {"gemm_fp64": 0, "gemm_tf32x3": 1, "permute": 2, "vector": 3, "skinny": 4,

@@ -43,7 +43,7 @@ def _flags():
 
 def _compile(src: str, extra=()) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    headers = glob.glob(os.path.join(CSRC, "*.hpp")) + \
+    headers = glob.glob(os.path.join(CSRC, "*.hpp")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         glob.glob(os.path.join(os.path.dirname(HERE), "include", "*.h"))
     newest = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in headers])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest:

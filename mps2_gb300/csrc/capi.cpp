@@ -493,6 +493,13 @@ int gq_profile_enable(int on) {
   });
 }
 
+int gq_host_sync_count(int64_t *count) {
+  return guarded([&] {
+    GQ_CHECK(count != nullptr, "null count");
+    *count = gq::host_sync_count();
+  });
+}
+
 int gq_profile_read(int kernel, int64_t *launches, double *ms, double *flops, double *bytes) {
   return guarded([&] {
     GQ_CHECK(kernel >= 0 && kernel < gq::kProfCount, "unknown kernel id");

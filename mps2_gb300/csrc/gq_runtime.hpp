@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
+
 #include <string>
 #include <vector>
 
@@ -67,7 +69,8 @@ Lane *lane_create();       // a new lane (own non-blocking stream)
 void lane_destroy(Lane *l);
 void lane_bind(Lane *l);   // bind to this thread (nullptr: the main lane)
 bool on_main_lane();
-void sync();
+void sync();                // wait for this thread's lane stream (counted)
+int64_t host_sync_count();  // waits by sync() since load, all threads
 
 // Kernel profiling with CUDA events on the library stream (off by default).
 enum ProfKernel : int {
@@ -304,12 +307,53 @@ void dev_lanczos_gamma(const double *x, const double *u, const double *a_dev,
 void dev_scale_rsqrt(double *x, int64_t n, const double *nrm2_dev);
 // x *= s
 void dev_scale(double *x, int64_t n, double s);
-// out = sum_k c[k] * bases[k]   (c on host, m vectors)
-void dev_combine(const std::vector<const double *> &bases, const std::vector<double> &c,
-                 double *out, int64_t n);
 // Block copies between structures: (src_off, dst_off, n) triples.
 void dev_block_copy(const double *src, double *dst, const std::vector<int64_t> &triples);
 int64_t dot_scratch_elems();
+
+// The Lanczos loop on the device (vecops.cu): its control block, the
+// buffers one iteration reads and writes, and the launches of one
+// iteration (the same launches for every iteration: they read the
+// iteration index from the control block).
+enum LzStatus : int {
+  kLzRunning = 0,
+  kLzConverged = 1,       // the stopping rule was met
+  kLzInvariant = 2,       // |gamma| == 0: the Krylov space is invariant
+  kLzBadVector = -1,      // non-finite Lanczos vector norm
+  kLzBadCoefficient = -2, // non-finite a_m or Ritz value
+  kLzCapped = -3,         // iteration cap of the device loop reached
+};
+struct LzCtl {
+  int m = 0;        // current iteration (vector v_m is being formed)
+  int status = 0;   // LzStatus
+  int nvec = 0;     // once stopped: Krylov vectors in the Ritz vector
+  int iters = 0;    // once stopped: iterations, as the reference counts them
+  int guard = 0;    // iterations executed by the device loop
+  int pad = 0;
+  double e0 = 0.0;      // lowest Ritz value of the previous iteration
+  double energy = 0.0;  // once stopped: the final Ritz value
+};
+struct LzLoop {
+  LzCtl *ctl = nullptr;
+  double *const *vecs = nullptr;  // device table: Krylov vector k at vecs[k]
+  double *xin = nullptr;          // copy of v_m for a matvec with a fixed input (or null)
+  double *w = nullptr;            // matvec output H v_m
+  int64_t n = 0;
+  double *a_dev = nullptr, *b_dev = nullptr, *n_dev = nullptr;  // a_m, b_m, |gamma_m|^2
+  double *c_dev = nullptr, *work = nullptr, *red = nullptr;     // Ritz coefficients, scratch
+  int maxit = 0;
+  int64_t dim = 0;
+  double error = 0.0;
+  int cap = 0;
+};
+using MatvecFn = std::function<void()>;
+void lz_init(LzCtl *ctl, const double *a_dev);  // m = 1, e0 = a_0
+// One iteration: b, v_m, w = H v_m (matvec), a_m, gamma_{m+1}, stopping
+// test; with set_cond the test also sets the graph's loop condition.
+void lz_iteration(const LzLoop &L, const MatvecFn &matvec, bool set_cond,
+                  cudaGraphConditionalHandle cond);
+// Ritz coefficients of the stopped loop and out = sum_k c_k v_k.
+void lz_ritz_vector(const LzLoop &L, double *out);
 
 // ---------------------------------------------------------------------------
 // Truncating SVD (svd.cu)
@@ -343,14 +387,6 @@ int pcmgs_max_rank();
 void launch_pcmgs(const PcGroup *groups_small, int n_small, const PcGroup *groups_big, int n_big,
                   const double *G, double *L, double *Q, double *T, double *C, int *r_small,
                   int *r_big, double tol);
-
-// ---------------------------------------------------------------------------
-// Tridiagonal eigensolver (tridiag.cpp)
-// ---------------------------------------------------------------------------
-// Lowest eigenvalue of the n x n symmetric tridiagonal matrix (diag a,
-// off-diag b); if vec != nullptr also its unit eigenvector (largest-|.|
-// component positive).  Returns false if the iteration fails to converge.
-bool tridiag_lowest(const double *a, const double *b, int n, double *eval, double *vec);
 
 // ---------------------------------------------------------------------------
 // Finite-MPS canonicalisation and truncation (mps.cu)

@@ -7,6 +7,14 @@
 // matvec follows ``eff_ham_mul_state_{cent,lend,rend}`` (``:228-256``)
 // contraction for contraction; its work lists are planned once per update
 // and replayed every iteration.
+//
+// The iteration itself runs on the device: the recurrence scalars, the
+// tridiagonal Ritz value (``TridiagGsSolver``, ``:259-313``) and the
+// stopping rule are computed by control kernels, so one iteration is a
+// fixed sequence of launches.  On the main lane that sequence is the body
+// of a CUDA-graph while loop and a whole solve costs one host wait; the
+// lanes of a batched run and profiled runs launch it once per iteration and
+// read the control block back after each.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -30,56 +38,31 @@ struct MatvecPlan {
   std::vector<TensorPtr> inter;
   DevBuf scratch;
   double flops = 0.0;
-  // The matvec's launch sequence is fixed for a whole Lanczos solve, so it
-  // is captured once as a CUDA graph reading a fixed input buffer and
-  // replayed every further iteration (captured lazily, for one (x, y) pair).
-  cudaGraphExec_t exec = nullptr;
-  const double *graph_x = nullptr;
-  double *graph_y = nullptr;
-  ~MatvecPlan() {
-    if (exec) cudaGraphExecDestroy(exec);
-  }
 };
 
 namespace {
-// Graph replay of the matvec on the main lane, unless the kernel profiler
-// is on (it times every launch with its own events) or GQ_NO_GRAPHS is set.
-// Not on the lanes of a batched run: there every solve's capture and
-// instantiation contend across the host threads (64 XXZ chains: 26.2 s with
-// graphs, 19.3 s without; one chain after another: 107 s vs 109 s).
+// The device loop runs as a CUDA graph on the main lane, unless the kernel
+// profiler is on (it times every launch with its own events, which a graph
+// body cannot hold) or GQ_NO_GRAPHS is set.  Not on the lanes of a batched
+// run: there every solve's graph build would contend across the host
+// threads (64 XXZ chains with graphed matvecs: 26.2 s, without: 19.3 s).
 bool graphs_enabled() {
   static const bool off = std::getenv("GQ_NO_GRAPHS") != nullptr;
   return !off && !prof_on() && on_main_lane();
 }
 
-void run_matvec_graph(MatvecPlan &p, const double *x, double *y, double *xin, int64_t n) {
-  auto s = stream();
-  if (!p.exec || p.graph_x != xin || p.graph_y != y) {
-    if (p.exec) {
-      GQ_CUDA(cudaGraphExecDestroy(p.exec));
-      p.exec = nullptr;
-    }
-    cudaGraph_t g = nullptr;
-    GQ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    try {
-      run_matvec(p, xin, y);
-    } catch (...) {
-      cudaGraph_t dead = nullptr;
-      cudaStreamEndCapture(s, &dead);
-      if (dead) cudaGraphDestroy(dead);
-      throw;
-    }
-    GQ_CUDA(cudaStreamEndCapture(s, &g));
-    const cudaError_t e = cudaGraphInstantiate(&p.exec, g, 0);
-    cudaGraphDestroy(g);
-    GQ_CUDA(e);
-    p.graph_x = xin;
-    p.graph_y = y;
+// A graph solve allocates every Krylov vector it may need up front; above
+// this many bytes the solve runs host-driven and allocates them one by one.
+constexpr double kGraphKrylovBytes = 48e9;
+
+struct GraphHolder {  // released on every exit path
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t e = nullptr;
+  ~GraphHolder() {
+    if (e) cudaGraphExecDestroy(e);
+    if (g) cudaGraphDestroy(g);
   }
-  if (x != xin)
-    GQ_CUDA(cudaMemcpyAsync(xin, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  GQ_CUDA(cudaGraphLaunch(p.exec, s));
-}
+};
 }  // namespace
 
 int64_t eff_ham_dim(const EffHam &h) {
@@ -252,144 +235,150 @@ void embed(const Tensor &src, Tensor &dst) {
   dev_block_copy(src.data.p, dst.data.p, tr);
 }
 
-namespace {
-// Copy `count` device scalars to the pinned host area and wait for them.
-void fetch(const double *dev, double *host, int count) {
-  GQ_CUDA(cudaMemcpyAsync(host, dev, sizeof(double) * count, cudaMemcpyDeviceToHost, stream()));
-  sync();
-}
-}  // namespace
-
 LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC &prm,
                       Precision prec) {
-  using clk = std::chrono::steady_clock;
   const int64_t maxit = prm.max_iterations;
   GQ_CHECK(maxit >= 2, "Lanczos needs max_iterations >= 2");
+  GQ_CHECK(maxit <= (1 << 20), "Lanczos max_iterations above 2^20");
   const int64_t n = init.size();
   GQ_CHECK(n > 0, "empty Lanczos vector");
   const int64_t dim = eff_ham_dim(h);
   auto plan = plan_matvec(h, init, prec);
+  // the split form reports the FP64 Rayleigh quotient of its ground state
+  const bool rayleigh = prec == kTF32x3 && prm.fp64_rayleigh;
+  auto p64 = rayleigh ? plan_matvec(h, init, prm.rayleigh) : nullptr;
+  auto s = stream();
+
+  // Krylov vectors: v_k for k < kmax at most (the loop stops at m == dim or
+  // m == maxit - 1 and writes gamma_{m+1} only while m + 1 < maxit).
+  const int64_t kmax = std::min<int64_t>(maxit, dim + 2);
+  const bool graph = graphs_enabled() && (double)kmax * (double)n * 8.0 <= kGraphKrylovBytes;
+  std::vector<DevBuf> vecs;
+  vecs.reserve(kmax);
+  std::vector<double *> table(kmax, nullptr);
+  auto add_vec = [&]() {
+    vecs.emplace_back(n);
+    table[vecs.size() - 1] = vecs.back().p;
+  };
+  add_vec();
+  add_vec();
+  if (graph)
+    while ((int64_t)vecs.size() < kmax) add_vec();
+  DevArray<double *> tab;
+  tab.upload(table);
+  DevBuf w(n), xin(graph ? n : 0), red(dot_scratch_elems()), rq(2);
+  // device scalars: a (maxit), b (maxit), |gamma|^2 (maxit + 1), Ritz
+  // coefficients (maxit), eigenvector scratch (5 maxit), control block
+  const int64_t ctl_doubles = (sizeof(LzCtl) + sizeof(double) - 1) / sizeof(double);
+  DevBuf sc(9 * maxit + 1 + ctl_doubles);
+  LzLoop L;
+  L.a_dev = sc.p;
+  L.b_dev = L.a_dev + maxit;
+  L.n_dev = L.b_dev + maxit;
+  L.c_dev = L.n_dev + maxit + 1;
+  L.work = L.c_dev + maxit;
+  L.ctl = reinterpret_cast<LzCtl *>(L.work + 5 * maxit);
+  L.vecs = tab.p;
+  L.xin = graph ? xin.p : nullptr;
+  L.w = w.p;
+  L.n = n;
+  L.red = red.p;
+  L.maxit = (int)maxit;
+  L.dim = dim;
+  L.error = prm.error;
+  L.cap = (int)maxit + 2;
 
   LanczosResult res;
-  std::vector<DevBuf> bases;
-  bases.reserve(maxit);
-  DevBuf last(n);
-  // device scalars: a[0..maxit), nrm2[0..maxit)
-  DevBuf sc(2 * maxit + 2);
-  double *a_dev = sc.p, *n_dev = sc.p + maxit;
-  DevBuf red(dot_scratch_elems());
-  std::vector<double> a(maxit, 0.0), b(maxit, 0.0), N(maxit, 0.0);
-  double *hs = lane().host_scalars;
-  const bool use_graph = graphs_enabled();
-  DevBuf xin(use_graph ? n : 0);
+  // v0 = init / |init|, w = H v0, a_0, gamma_1 (``lanczos_solver_impl.h:120-160``)
+  double *v0 = table[0];
+  GQ_CUDA(cudaMemcpyAsync(v0, init.data.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  dev_dot(v0, v0, n, L.n_dev, red.p);
+  dev_scale_rsqrt(v0, n, L.n_dev);
+  run_matvec(*plan, v0, w.p);
+  dev_dot(v0, w.p, n, L.a_dev, red.p);
+  dev_lanczos_gamma(w.p, v0, L.a_dev, nullptr, nullptr, true, table[1], n, L.n_dev + 1, red.p);
+  lz_init(L.ctl, L.a_dev);
 
-  // A solve that converges within two matvecs (the common case once a
-  // sweep has converged) never pays for capturing and instantiating the
-  // graph; longer solves replay it from the third matvec on.
-  auto matvec = [&](const double *x) {
-    if (use_graph && res.matvecs >= 2)
-      run_matvec_graph(*plan, x, last.p, xin.p, n);
-    else
-      run_matvec(*plan, x, last.p);
-    res.matvecs++;
-    res.matvec_flops += plan->flops;
-  };
-
-  // One host round trip per iteration: right after <v_m, H v_m> the next
-  // recurrence vector gamma_{m+1} and its squared norm are formed on the
-  // device, and both scalars come back together.  If the iteration turns
-  // out to be the last one, that speculative vector is simply unused.
-  auto gamma_step = [&](int64_t m1) {  // bases[m1] = last - a[m1-1] v_{m1-1} - b v_{m1-2}
-    while ((int64_t)bases.size() <= m1) bases.emplace_back(n);
-    dev_lanczos_gamma(last.p, bases[m1 - 1].p, a_dev + (m1 - 1),
-                      m1 >= 2 ? bases[m1 - 2].p : nullptr, m1 >= 2 ? n_dev + (m1 - 1) : nullptr,
-                      true, bases[m1].p, n, n_dev + m1, red.p);
-  };
-  auto fetch2 = [&](int64_t m_a) {  // a[m_a] and nrm2[m_a + 1] -> hs[0], hs[1]
-    GQ_CUDA(cudaMemcpyAsync(hs, a_dev + m_a, sizeof(double), cudaMemcpyDeviceToHost, stream()));
-    GQ_CUDA(cudaMemcpyAsync(hs + 1, n_dev + m_a + 1, sizeof(double), cudaMemcpyDeviceToHost,
-                            stream()));
-    sync();
-  };
-
-  // v0 = init / |init|
-  bases.emplace_back(n);
-  GQ_CUDA(cudaMemcpyAsync(bases[0].p, init.data.p, sizeof(double) * n, cudaMemcpyDeviceToDevice,
-                          stream()));
-  dev_dot(bases[0].p, bases[0].p, n, n_dev, red.p);
-  dev_scale_rsqrt(bases[0].p, n, n_dev);
-  matvec(bases[0].p);
-  dev_dot(bases[0].p, last.p, n, a_dev, red.p);
-  gamma_step(1);
-  fetch2(0);
-  a[0] = hs[0];
-  double nrm2_next = hs[1];
-  double energy0 = a[0];
-
-  auto finish = [&](int64_t nvec, int64_t iters, double energy) {
-    std::vector<double> c(nvec, 1.0);
-    if (nvec > 1) {
-      double ev;
-      if (!tridiag_lowest(a.data(), b.data(), (int)nvec, &ev, c.data()))
-        fail(kNumericalError, "tridiagonal eigensolver did not converge");
+  LzCtl *hc = reinterpret_cast<LzCtl *>(lane().host_scalars);
+  if (graph) {
+    GraphHolder G;
+    GQ_CUDA(cudaGraphCreate(&G.g, 0));
+    cudaGraphConditionalHandle cond;
+    GQ_CUDA(cudaGraphConditionalHandleCreate(&cond, G.g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    GQ_CUDA(cudaGraphAddNode(&node, G.g, nullptr, nullptr, 0, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    GQ_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal));
+    try {
+      lz_iteration(L, [&]() { run_matvec(*plan, xin.p, w.p); }, true, cond);
+    } catch (...) {
+      cudaGraph_t dead = nullptr;
+      cudaStreamEndCapture(s, &dead);
+      throw;
     }
-    auto gs = clone_structure(init);
-    gs->allocate();
-    std::vector<const double *> ptrs;
-    for (int64_t k = 0; k < nvec; ++k) ptrs.push_back(bases[k].p);
-    dev_combine(ptrs, c, gs->data.p, n);
-    res.iters = iters;
-    res.energy = energy;
-    res.ritz_energy = energy;
-    res.gs = gs;
-    if (prec == kTF32x3 && prm.fp64_rayleigh) {
-      // FP64 Rayleigh quotient of the split-precision ground state
-      auto p64 = plan_matvec(h, init, prm.rayleigh);
-      run_matvec(*p64, gs->data.p, last.p);
-      dev_dot(gs->data.p, last.p, n, a_dev, red.p);
-      dev_dot(gs->data.p, gs->data.p, n, n_dev, red.p);
-      GQ_CUDA(cudaMemcpyAsync(hs, a_dev, sizeof(double), cudaMemcpyDeviceToHost, stream()));
-      GQ_CUDA(cudaMemcpyAsync(hs + 1, n_dev, sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    cudaGraph_t captured = nullptr;
+    GQ_CUDA(cudaStreamEndCapture(s, &captured));
+    GQ_CUDA(cudaGraphInstantiate(&G.e, G.g, 0));
+    GQ_CUDA(cudaGraphLaunch(G.e, s));
+  } else {
+    for (int m = 1;; ) {
+      // gamma_{m+1} is written this iteration: its vector must exist
+      if (m + 1 < kmax && (int64_t)vecs.size() <= m + 1) {
+        add_vec();
+        upload_async(tab.p + m + 1, &table[m + 1], sizeof(double *));
+      }
+      double *vm = table[m];
+      lz_iteration(L, [&]() { run_matvec(*plan, vm, w.p); }, false, 0);
+      GQ_CUDA(cudaMemcpyAsync(hc, L.ctl, sizeof(LzCtl), cudaMemcpyDeviceToHost, s));
       sync();
-      res.energy = hs[0] / hs[1];
-      res.matvecs++;
-      res.matvec_flops += p64->flops;
+      if (hc->status != kLzRunning) break;
+      m = hc->m;
     }
-  };
+  }
 
-  int64_t m = 0;
-  while (true) {
-    m += 1;
-    const double nrm2 = nrm2_next;
-    if (!std::isfinite(nrm2)) fail(kNumericalError, "Lanczos vector became non-finite");
-    const double norm_gamma = std::sqrt(nrm2);
-    if (norm_gamma == 0.0) {  // invariant subspace found
-      finish(m, m, energy0);
+  // Ritz vector, the Rayleigh quotient, and one read-back of the results
+  auto gs = clone_structure(init);
+  gs->allocate();
+  lz_ritz_vector(L, gs->data.p);
+  if (rayleigh) {
+    run_matvec(*p64, gs->data.p, w.p);
+    dev_dot(gs->data.p, w.p, n, rq.p, red.p);
+    dev_dot(gs->data.p, gs->data.p, n, rq.p + 1, red.p);
+  }
+  double *hs = lane().host_scalars + ctl_doubles;
+  GQ_CUDA(cudaMemcpyAsync(hc, L.ctl, sizeof(LzCtl), cudaMemcpyDeviceToHost, s));
+  if (rayleigh)
+    GQ_CUDA(cudaMemcpyAsync(hs, rq.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  sync();
+  const LzCtl c = *hc;
+  switch (c.status) {
+    case kLzConverged:
+    case kLzInvariant:
       break;
-    }
-    N[m] = nrm2;
-    b[m - 1] = norm_gamma;
-    dev_scale_rsqrt(bases[m].p, n, n_dev + m);
-    matvec(bases[m].p);
-    dev_dot(bases[m].p, last.p, n, a_dev + m, red.p);
-    const bool more = m + 1 < maxit;
-    if (more) gamma_step(m + 1);
-    if (more) {
-      fetch2(m);
-      nrm2_next = hs[1];
-    } else {
-      fetch(a_dev + m, hs, 1);
-    }
-    a[m] = hs[0];
-    if (!std::isfinite(a[m])) fail(kNumericalError, "Lanczos coefficient became non-finite");
-    double e_new;
-    if (!tridiag_lowest(a.data(), b.data(), (int)(m + 1), &e_new, nullptr))
-      fail(kNumericalError, "tridiagonal eigensolver did not converge");
-    if ((energy0 - e_new) < prm.error || m == dim || m == maxit - 1) {
-      finish(m + 1, m, e_new);
-      break;
-    }
-    energy0 = e_new;
+    case kLzBadVector:
+      fail(kNumericalError, "Lanczos vector became non-finite");
+    case kLzBadCoefficient:
+      fail(kNumericalError, "Lanczos coefficient became non-finite");
+    default:
+      fail(kNumericalError, "Lanczos loop stopped without meeting its stopping rule (status " +
+                                std::to_string(c.status) + ")");
+  }
+  res.iters = c.iters;
+  res.energy = c.energy;
+  res.ritz_energy = c.energy;
+  res.gs = gs;
+  res.matvecs = 1 + c.guard;
+  res.matvec_flops = plan->flops * (double)(1 + c.guard);
+  if (rayleigh) {
+    res.energy = hs[0] / hs[1];
+    res.matvecs++;
+    res.matvec_flops += p64->flops;
   }
   return res;
 }

@@ -2,6 +2,7 @@
 #include "gq_runtime.hpp"
 
 #include <cstdio>
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <map>
@@ -150,7 +151,14 @@ void upload_async(void *dst, const void *src, size_t bytes) {
   l.staging_head = off + bytes;
 }
 
+namespace {
+std::atomic<int64_t> g_host_syncs{0};
+}  // namespace
+
+int64_t host_sync_count() { return g_host_syncs.load(); }
+
 void sync() {
+  g_host_syncs.fetch_add(1, std::memory_order_relaxed);
   if (!prof_on()) {
     GQ_CUDA(cudaStreamSynchronize(stream()));
     return;

@@ -211,6 +211,13 @@ def profile_read(kernel: str):
     return n.value, ms.value, fl.value, by.value
 
 
+def host_sync_count() -> int:
+    """Host waits on the library's streams since it was loaded."""
+    n = C.c_int64()
+    check(load().gq_host_sync_count(C.byref(n)))
+    return n.value
+
+
 def library_stream() -> int:
     s = C.c_void_p()
     check(load().gq_get_stream(C.byref(s)))

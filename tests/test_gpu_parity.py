@@ -133,25 +133,48 @@ def test_lanczos_matches_oracle(lib, where):
     assert rel_err(a * s, ref.gs_vec) <= 1e-6
 
 
-@pytest.mark.parametrize("prec", ["fp64", "tf32x3"])
-def test_lanczos_graph_replay_matches_launch_by_launch(lib, prec):
-    """The matvec replayed as a CUDA graph (default) and launched kernel by
-    kernel (what the kernel profiler forces) run the same kernels in the
-    same order: identical energies and ground states."""
-    from mps2_gb300.vmps import LanczosParams, LanczosSolver, profile_enable
+@pytest.mark.parametrize("prec", ["fp64", "tf32x3", "fp64tc"])
+def test_lanczos_device_loop_matches_host_driven_loop(lib, prec):
+    """The Lanczos iteration run as a CUDA-graph while loop on the device
+    (default) and driven from the host one iteration at a time (what the
+    kernel profiler forces) launch the same kernels in the same order:
+    bitwise identical energies, iteration counts and ground states.  The
+    device loop waits on the host once per solve, the host-driven one once
+    more per iteration."""
+    from mps2_gb300.vmps import LanczosParams, LanczosSolver, host_sync_count, profile_enable
     from test_oracle_golden import _random_sym_env
     rng = np.random.default_rng(8)
     eff, theta = _random_sym_env(rng, 160, 2, 2)
     eff = [from_oracle(t) for t in eff]
     theta = from_oracle(theta)
     lp = LanczosParams(1e-12, 40)
+    c0 = host_sync_count()
     a = LanczosSolver(eff, theta, lp, "cent", precision=prec)
+    c1 = host_sync_count()
     profile_enable(True)
     b = LanczosSolver(eff, theta, lp, "cent", precision=prec)
+    c2 = host_sync_count()
     profile_enable(False)
-    assert a.iters == b.iters
+    assert a.iters == b.iters and a.iters >= 10
     assert a.gs_eng == b.gs_eng
     assert rel_err(a.gs_vec, to_oracle(b.gs_vec)) == 0.0
+    assert (c2 - c1) - (c1 - c0) == a.iters
+    assert c1 - c0 <= 4
+
+
+def test_lanczos_device_loop_stops_at_max_iterations(lib):
+    """A solve that cannot meet its tolerance stops after max_iterations - 1
+    iterations (``lanczos_solver_impl.h:205-219``), in the device loop as on
+    the oracle."""
+    from mps2_gb300.vmps import LanczosParams, LanczosSolver
+    from test_oracle_golden import _random_sym_env
+    rng = np.random.default_rng(9)
+    eff, theta = _random_sym_env(rng, 120, 2, 2)
+    ref = oracle.lanczos_solver(eff, theta, OLP(0.0, 7), "cent")
+    got = LanczosSolver([from_oracle(t) for t in eff], from_oracle(theta),
+                        LanczosParams(0.0, 7), "cent")
+    assert got.iters == ref.iters == 6
+    assert abs(got.gs_eng - ref.gs_eng) <= 1e-10 * abs(ref.gs_eng)
 
 
 def test_lanczos_vs_dense_diagonalisation(lib):
