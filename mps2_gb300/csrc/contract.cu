@@ -15,8 +15,11 @@
 // permute kernel reorders all of its blocks first.
 #include <array>
 #include <chrono>
+#include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
+#include <unordered_map>
 
 #include "gq_runtime.hpp"
 
@@ -96,6 +99,116 @@ void run_perm(const PermPlan &pp, const double *src, double *dst) {
 
 }  // namespace
 
+namespace {
+std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
+                                         const std::vector<int> &axes_a,
+                                         const std::vector<int> &axes_b, const Tensor *target,
+                                         Precision prec, double tc_frac);
+
+// 128-bit fingerprint of a plan's inputs: two independent 64-bit mixes
+// (FNV-1a and a splitmix64 chain) over every structural word.
+struct Fingerprint {
+  uint64_t h0 = 1469598103934665603ull, h1 = 0x243f6a8885a308d3ull;
+  void add(uint64_t x) {
+    h0 = (h0 ^ x) * 1099511628211ull;
+    uint64_t z = h1 + x + 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    h1 = z ^ (z >> 31);
+  }
+  void add_tensor(const Tensor &t) {
+    add((uint64_t)t.nq);
+    add((uint64_t)t.rank());
+    for (const Index &ix : t.idx) {
+      add((uint64_t)(int64_t)ix.dir);
+      add((uint64_t)ix.qn.size());
+      for (size_t k = 0; k < ix.qn.size(); ++k) {
+        for (int q = 0; q < t.nq; ++q) add((uint64_t)(int64_t)ix.qn[k].v[q]);
+        add((uint64_t)ix.dim[k]);
+      }
+    }
+    for (int q = 0; q < t.nq; ++q) add((uint64_t)(int64_t)t.div.v[q]);
+    add((uint64_t)t.nblocks());
+    for (int c : t.coords) add((uint64_t)(int64_t)c);
+  }
+};
+
+struct PlanKey {
+  uint64_t h0, h1;
+  bool operator==(const PlanKey &o) const { return h0 == o.h0 && h1 == o.h1; }
+};
+struct PlanKeyHash {
+  size_t operator()(const PlanKey &k) const { return (size_t)k.h0; }
+};
+
+int64_t plan_device_bytes(const ContractPlan &p) {
+  auto arr = [](const auto &d) { return d.n * (int64_t)sizeof(*d.p); };
+  return arr(p.sk_items) + arr(p.sk_pairs) + arr(p.tiles) + arr(p.pairs) + arr(p.tiles_tc) +
+         arr(p.pairs_tc) + arr(p.tiles_oz) + arr(p.pairs_oz) + arr(p.zero_blocks) +
+         arr(p.pa.blocks) + arr(p.pa.chunks) + arr(p.pb.blocks) + arr(p.pb.chunks) +
+         arr(p.ta.blocks_dev) + arr(p.ta.tasks_dev) + arr(p.tb.blocks_dev) +
+         arr(p.tb.tasks_dev) + arr(p.oa.blocks_dev) + arr(p.oa.tasks_dev) +
+         arr(p.ob.blocks_dev) + arr(p.ob.tasks_dev);
+}
+
+void release_operand_packs(ContractPlan &p) {
+  p.a_packed.release();
+  p.b_packed.release();
+  p.a_oz.release();
+  p.b_oz.release();
+  p.a_cached = p.b_cached = p.a_oz_cached = p.b_oz_cached = false;
+}
+
+constexpr size_t kPlanCacheEntries = 8192;
+constexpr int64_t kPlanCacheBytes = int64_t(8) << 30;  // device work lists
+}  // namespace
+
+struct PlanCache {
+  struct Entry {
+    std::shared_ptr<ContractPlan> plan;
+    bool in_use = false;
+    uint64_t last = 0;
+    int64_t bytes = 0;
+  };
+  std::unordered_map<PlanKey, Entry, PlanKeyHash> map;
+  uint64_t tick = 0;
+  int64_t bytes = 0;
+
+  // Least recently used entries not in use go first.
+  void make_room(int64_t need) {
+    while (!map.empty() && (map.size() >= kPlanCacheEntries || bytes + need > kPlanCacheBytes)) {
+      auto victim = map.end();
+      for (auto it = map.begin(); it != map.end(); ++it)
+        if (!it->second.in_use && (victim == map.end() || it->second.last < victim->second.last))
+          victim = it;
+      if (victim == map.end()) return;
+      bytes -= victim->second.bytes;
+      map.erase(victim);
+    }
+  }
+};
+
+namespace {
+// The holder's handle on a cached plan: when the last copy goes, the plan's
+// operand packs are released and the entry may be handed out again.
+std::shared_ptr<ContractPlan> lend(const std::shared_ptr<PlanCache> &cache, const PlanKey &key,
+                                   PlanCache::Entry &e) {
+  e.in_use = true;
+  e.last = ++cache->tick;
+  std::shared_ptr<ContractPlan> master = e.plan;
+  return std::shared_ptr<ContractPlan>(master.get(), [cache, key, master](ContractPlan *p) {
+    release_operand_packs(*p);
+    auto it = cache->map.find(key);
+    if (it != cache->map.end() && it->second.plan.get() == p) it->second.in_use = false;
+  });
+}
+
+bool plan_cache_on() {
+  static const bool off = std::getenv("GQ_NO_PLAN_CACHE") != nullptr;
+  return !off;
+}
+}  // namespace
+
 std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
                                             const std::vector<int> &axes_a,
                                             const std::vector<int> &axes_b,
@@ -108,6 +221,44 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
                 std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
     }
   } plan_timer;
+  if (!plan_cache_on()) return build_plan(a, b, axes_a, axes_b, target, prec, tc_frac);
+  Fingerprint f;
+  f.add(0x706c616e31ull);  // layout version of the key
+  f.add_tensor(a);
+  f.add_tensor(b);
+  f.add(axes_a.size());
+  for (int x : axes_a) f.add((uint64_t)(int64_t)x);
+  for (int x : axes_b) f.add((uint64_t)(int64_t)x);
+  f.add(target ? 1 : 0);
+  if (target) f.add_tensor(*target);
+  f.add((uint64_t)prec);
+  uint64_t fb;
+  std::memcpy(&fb, &tc_frac, sizeof(fb));
+  f.add(fb);
+  const PlanKey key{f.h0, f.h1};
+  Lane &l = lane();
+  if (!l.plan_cache) l.plan_cache = std::make_shared<PlanCache>();
+  auto &cache = l.plan_cache;
+  auto it = cache->map.find(key);
+  if (it != cache->map.end()) {
+    if (!it->second.in_use) return lend(cache, key, it->second);
+    return build_plan(a, b, axes_a, axes_b, target, prec, tc_frac);  // held: a private plan
+  }
+  auto p = build_plan(a, b, axes_a, axes_b, target, prec, tc_frac);
+  const int64_t bytes = plan_device_bytes(*p);
+  cache->make_room(bytes);
+  auto &e = cache->map[key];
+  e.plan = p;
+  e.bytes = bytes;
+  cache->bytes += bytes;
+  return lend(cache, key, e);
+}
+
+namespace {
+std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
+                                         const std::vector<int> &axes_a,
+                                         const std::vector<int> &axes_b, const Tensor *target,
+                                         Precision prec, double tc_frac) {
   const int ra = a.rank(), rb = b.rank(), nc = (int)axes_a.size();
   GQ_CHECK(nc == (int)axes_b.size() && nc >= 1, "contraction needs matching, non-empty axes");
   GQ_CHECK(a.nq == b.nq, "operands use different charge counts");
@@ -479,6 +630,7 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   plan->b_elems = b.size();
   return plan;
 }
+}  // namespace
 
 namespace {
 int64_t floats_as_doubles(int64_t f) { return (f + 1) / 2 + 8; }  // + slack for alignment

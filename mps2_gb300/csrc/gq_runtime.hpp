@@ -17,6 +17,7 @@ namespace gq {
 // thread uses the context's main lane unless it has bound its own, which
 // is how independent DMRG instances run concurrently (one host thread and
 // one stream each).
+struct PlanCache;  // contract.cu
 struct Lane {
   cudaStream_t stream = nullptr;
   double *host_scalars = nullptr;  // pinned, 64 doubles
@@ -34,6 +35,8 @@ struct Lane {
   void *aux_cusolver[kAux] = {};  // cusolverDnHandle_t on aux_stream[i]
   cudaEvent_t fork_event = nullptr;
   cudaEvent_t join_event[kAux] = {};
+  // Contraction plans of this lane, kept by structure (contract.cu).
+  std::shared_ptr<PlanCache> plan_cache;
 };
 
 struct Context {
@@ -226,6 +229,12 @@ struct ContractPlan {
 // `tc_frac` < 0: the default share of useful work at which an output block
 // goes to the tensor-core kernel (2% for 3xTF32, 3% for FP64TC); otherwise
 // that share (an autotuned value).
+//
+// Plans are kept per lane and handed out again for a contraction with the
+// same block structures, axes, arithmetic and threshold (a sweep at fixed D
+// meets every bond's structures again); a plan is never handed to two
+// holders at once, and the operand packs of cache_operand are released when
+// its holder lets it go.  GQ_NO_PLAN_CACHE turns the cache off.
 std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
                                             const std::vector<int> &axes_a,
                                             const std::vector<int> &axes_b,

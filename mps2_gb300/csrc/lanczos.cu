@@ -244,9 +244,10 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   GQ_CHECK(n > 0, "empty Lanczos vector");
   const int64_t dim = eff_ham_dim(h);
   auto plan = plan_matvec(h, init, prec);
-  // the split form reports the FP64 Rayleigh quotient of its ground state
+  // the split form reports the FP64 Rayleigh quotient of its ground state;
+  // its matvec is planned while the device iterates
   const bool rayleigh = prec == kTF32x3 && prm.fp64_rayleigh;
-  auto p64 = rayleigh ? plan_matvec(h, init, prm.rayleigh) : nullptr;
+  std::shared_ptr<MatvecPlan> p64;
   auto s = stream();
 
   // Krylov vectors: v_k for k < kmax at most (the loop stops at m == dim or
@@ -343,6 +344,7 @@ LanczosResult lanczos(const EffHam &h, const Tensor &init, const LanczosParamsC 
   }
 
   // Ritz vector, the Rayleigh quotient, and one read-back of the results
+  if (rayleigh) p64 = plan_matvec(h, init, prm.rayleigh);
   auto gs = clone_structure(init);
   gs->allocate();
   lz_ritz_vector(L, gs->data.p);
