@@ -105,9 +105,10 @@ def _args():
                    help="timed sweeps of the plain FP64 form after the split ones")
     p.add_argument("--autotune", action="store_true",
                    help="enable the tile-choice autotuner (gq_autotune_enable) for the run")
-    p.add_argument("--profile-region", choices=["sweeps", "centre"], default="sweeps",
+    p.add_argument("--profile-region", choices=["sweeps", "centre", "update"], default="sweeps",
                    help="what an external profiler started with --profile-from-start off "
-                        "records: the timed sweeps, or the centre bond's Lanczos solves")
+                        "records: the timed sweeps, the centre bond's Lanczos solves in the "
+                        "three forms, or the split form's two-site update at the centre bond")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--record-structure", action="store_true",
                    help="write the block structures of the sampled bonds (reference arm)")
@@ -518,7 +519,13 @@ def run_ours(args):
                                "kernel_ms": {k: pr[k][1] for k in FAMILIES},
                                "matvec_gemm_tflops": gemm_fl / (gemm_ms * 1e-3) / 1e12
                                if gemm_ms else None}
+        if b == centre and args.profile_region == "update":
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
         g = st.update(params(D), "r", b)
+        if b == centre and args.profile_region == "update":
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
         i = b + 1
         if b == centre:
             gpu_centre = g
