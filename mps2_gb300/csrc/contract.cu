@@ -335,7 +335,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
   // must be small in absolute terms and tiny next to A, so a two-site state
   // contracted with an environment never lands here.
   if (skinny_eligible_sizes(a.size(), b.size())) {
-    int64_t max_k = 0, max_n = 0;
+    int64_t max_k = 0, max_n = 0, kn = 0;
     for (auto &kv : out) {
       int64_t n = 1;
       for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
@@ -344,9 +344,12 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
         int64_t k = 1;
         for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
         max_k = std::max(max_k, k);
+        kn += k * n;
       }
     }
-    if (skinny_eligible(b, max_k, max_n) && (int)free_a.size() <= skinny_max_free_legs()) {
+    // the plan lists every pair's (k, j) B offsets: keep that list small
+    if (skinny_eligible(b, max_k, max_n) && (int)free_a.size() <= skinny_max_free_legs() &&
+        kn <= (int64_t(1) << 26)) {
       auto strides = [](const Tensor &t, int64_t blk, int64_t *str) {
         int64_t s = 1;
         for (int l = t.rank() - 1; l >= 0; --l) {
@@ -356,12 +359,26 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       };
       std::vector<SkinnyPair> sp;
       std::vector<SkinnyItem> items;
+      std::vector<int64_t> koffs;
+      std::vector<int> bidx;
       std::vector<char> touched(o.nblocks(), 0);
       const int rows = skinny_rows_per_cta();
-      auto add_items = [&](int64_t c_off, int64_t m, int64_t n, int pb, int pe) {
-        for (int64_t r0 = 0; r0 < m; r0 += rows)
-          items.push_back({c_off, (int)m, (int)n, (int)r0, pb, pe});
+      auto add_items = [&](int64_t c_off, int64_t m, int64_t n, int pb, int pe,
+                           const int *fdims, int nf) {
+        for (int64_t r0 = 0; r0 < m; r0 += rows) {
+          SkinnyItem it{};
+          it.c_off = c_off;
+          it.M = (int)m;
+          it.N = (int)n;
+          it.row0 = (int)r0;
+          it.pair_begin = pb;
+          it.pair_end = pe;
+          it.nfa = nf;
+          for (int t = 0; t < kSkMaxFree; ++t) it.fa_dims[t] = t < nf ? fdims[t] : 1;
+          items.push_back(it);
+        }
       };
+      const int nfree = (int)free_a.size();
       for (auto &kv : out) {
         const int64_t ob = o.find(kv.first.data());
         GQ_CHECK(ob >= 0, "contraction produces a block missing from the target structure");
@@ -370,35 +387,55 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
         for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
         for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
         const int pb = (int)sp.size();
+        int fdims[kSkMaxFree] = {1, 1, 1, 1};
         for (auto &cp : kv.second) {
           int64_t sa[kMaxRank], sb[kMaxRank];
           strides(a, cp.ablk, sa);
           strides(b, cp.bblk, sb);
           SkinnyPair q{};
           q.a_off = a.offs[cp.ablk];
-          q.b_off = b.offs[cp.bblk];
-          q.nk = nc;
           q.K = 1;
-          for (int t = 0; t < nc; ++t) {
-            q.k_dims[t] = (int)a.block_dim(cp.ablk, axes_a[t]);
-            q.ka_str[t] = sa[axes_a[t]];
-            q.kb_str[t] = sb[axes_b[t]];
-            q.K *= q.k_dims[t];
-          }
-          q.nfa = (int)free_a.size();
-          for (size_t t = 0; t < free_a.size(); ++t) {
-            q.fa_dims[t] = (int)a.block_dim(cp.ablk, free_a[t]);
+          for (int t = 0; t < nc; ++t) q.K *= (int)a.block_dim(cp.ablk, axes_a[t]);
+          for (int t = 0; t < nfree; ++t) {
+            fdims[t] = (int)a.block_dim(cp.ablk, free_a[t]);
             q.fa_str[t] = sa[free_a[t]];
           }
-          q.nfb = (int)free_b.size();
-          for (size_t t = 0; t < free_b.size(); ++t) {
-            q.fb_dims[t] = (int)b.block_dim(cp.bblk, free_b[t]);
-            q.fb_str[t] = sb[free_b[t]];
+          // A offsets of the contracted indices, last contracted leg fastest
+          q.koff = (int)koffs.size();
+          for (int e = 0; e < q.K; ++e) {
+            int rem = e;
+            int64_t oa = 0;
+            for (int t = nc - 1; t >= 0; --t) {
+              const int d = (int)a.block_dim(cp.ablk, axes_a[t]);
+              oa += (int64_t)(rem % d) * sa[axes_a[t]];
+              rem /= d;
+            }
+            koffs.push_back(oa);
+          }
+          // B offsets of the (k, j) values, j over B's free legs (last fastest)
+          q.bidx = (int)bidx.size();
+          for (int e = 0; e < q.K; ++e) {
+            int rem = e;
+            int64_t obk = b.offs[cp.bblk];
+            for (int t = nc - 1; t >= 0; --t) {
+              const int d = (int)b.block_dim(cp.bblk, axes_b[t]);
+              obk += (int64_t)(rem % d) * sb[axes_b[t]];
+              rem /= d;
+            }
+            for (int64_t j = 0; j < n; ++j) {
+              int64_t rj = j, o2 = obk;
+              for (int t = (int)free_b.size() - 1; t >= 0; --t) {
+                const int64_t d = b.block_dim(cp.bblk, free_b[t]);
+                o2 += (rj % d) * sb[free_b[t]];
+                rj /= d;
+              }
+              bidx.push_back((int)o2);
+            }
           }
           sp.push_back(q);
           plan->flops += 2.0 * (double)m * (double)n * (double)q.K;
         }
-        add_items(o.offs[ob], m, n, pb, (int)sp.size());
+        add_items(o.offs[ob], m, n, pb, (int)sp.size(), fdims, nfree);
       }
       for (int64_t ob = 0; ob < o.nblocks(); ++ob) {
         if (touched[ob]) continue;
@@ -406,14 +443,18 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
         int64_t m = 1, n = 1;
         for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[c[l]];
         for (size_t l = nfa; l < o.idx.size(); ++l) n *= o.idx[l].dim[c[l]];
-        add_items(o.offs[ob], m, n, 0, 0);
+        int fdims[kSkMaxFree] = {1, 1, 1, 1};
+        for (int t = 0; t < nfree; ++t) fdims[t] = (int)o.idx[t].dim[c[t]];
+        add_items(o.offs[ob], m, n, 0, 0, fdims, nfree);
         plan->nzero_blocks++;
       }
       plan->use_skinny = true;
-      plan->sk_jb = max_n <= 8 ? 8 : (max_n <= 16 ? 16 : 32);
+      plan->sk_jb = max_n <= 2 ? 2 : max_n <= 4 ? 4 : max_n <= 8 ? 8 : max_n <= 16 ? 16 : 32;
       plan->sk_nitems = (int64_t)items.size();
       plan->sk_items.upload(items);
       plan->sk_pairs.upload(sp);
+      plan->sk_koffs.upload(koffs);
+      plan->sk_bidx.upload(bidx);
       plan->a_elems = a.size();
       plan->b_elems = b.size();
       return plan;
@@ -444,7 +485,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       const int TN = prec == kTF32x3 ? 128 : oz_tile_n();
       const double frac = tc_frac >= 0.0 ? tc_frac : (prec == kTF32x3 ? 0.02 : 0.03);
       plan->tc_frac = frac;
-      double useful = 0.0, padded = 0.0;
+      double useful = 0.0, padded = 0.0, padded_fp64 = 0.0;
       int64_t ksum = 0;
       for (auto &cp : kv.second) {
         int64_t k = 1;
@@ -452,9 +493,18 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
         useful += 2.0 * m * n * k;
         padded += 2.0 * (double)((m + TM - 1) / TM * TM) * (double)((n + TN - 1) / TN * TN) *
                   ((k + 31) / 32 * 32.0);
+        padded_fp64 += 2.0 * (double)((m + 63) / 64 * 64) * (double)((n + 63) / 64 * 64) * k;
         ksum += (k + 31) / 32 * 32;
       }
       tc = useful >= frac * padded;
+      // In the FP64-accurate form a block also goes to the tensor cores by
+      // default when their padded work costs less time than the FP64
+      // kernel's padded 64 x 64 tiles: thin blocks (a few rows or columns,
+      // long k) waste most of either tile, and the FP64 pipe of this part is
+      // ~20x slower than that form.  (The split form keeps thin blocks in
+      // FP64: moved to 3xTF32 they shift its Lanczos convergence enough to
+      // leave the per-sweep energy parity of 1e-9 on transient sweeps.)
+      if (prec == kFP64TC && tc_frac < 0.0 && padded < 20.0 * padded_fp64) tc = true;
       // the FP64-accurate kernel's exact running sums cover k <= oz_max_k()
       if (prec == kFP64TC && ksum > oz_max_k()) tc = false;
       if (tc) plan->padded_flops += padded;

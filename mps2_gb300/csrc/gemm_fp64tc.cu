@@ -57,6 +57,32 @@ constexpr int kAStage = kSlices * kATile;     // 56 KB
 constexpr int kBStage = kSlices * kBTile;     // 42 KB
 constexpr int kStageBytes = kAStage + kBStage;
 constexpr int kChunkSteps = 8;                // 256 k between read-outs
+
+// The merge turns FP32 accumulator values into int64 running sums.  The
+// hardware float-to-int64 conversion issues on the FP64 pipe, which on this
+// part runs ~2 operations per clock per SM (61k conversions per 256-k chunk
+// of a 128 x 96 tile would outlast the chunk's MMAs), so both steps below
+// use the FP32 and integer pipes only.
+//
+// x rounded to the nearest integer, ties to even: adding and removing 2^23
+// with the sign of x rounds a float of magnitude below 2^23 (FP32 adds round
+// to nearest even); larger floats are integers already.
+__device__ __forceinline__ float round_f32(float x) {
+  const float big = 8388608.0f;  // 2^23
+  if (!(fabsf(x) < big)) return x;
+  return x >= 0.0f ? (x + big) - big : (x - big) + big;
+}
+// An integer-valued float (|x| < 2^63) as int64, from its bits: the
+// significand shifted by the exponent.
+__device__ __forceinline__ long long integral_f32_to_i64(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const int e = (int)((u >> 23) & 0xffu);
+  if (e < 127) return 0;  // |x| < 1: zero (x is an integer)
+  const uint64_t m = (uint64_t)((u & 0x7fffffu) | 0x800000u);
+  const int sh = e - 150;  // x = m 2^sh, sh >= -23
+  const uint64_t mag = sh >= 0 ? (m << (sh < 39 ? sh : 39)) : (m >> -sh);
+  return (u >> 31) ? -(long long)mag : (long long)mag;
+}
 constexpr int kThreads = 320;          // 8 merge warps, producer, MMA issuer
 constexpr int kMergeThreads = 256;
 constexpr int kMaxK = 1 << 16;          // k of one tile, summed over its pairs
@@ -450,11 +476,15 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
           uint32_t f[16];
           OZ_LD16(tmem + lane_base + (uint32_t)(a * oz::BN + cbase + cb * 16), f);
           tc_wait_ld();
+          if (a < oz::kAcc - 1) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            // orders 0..3: x * 2^30 is an exact integer; order 4..6: rounded
-            const float x = __uint_as_float(f[j]) * two30;
-            run[cb * 16 + j] += a < oz::kAcc - 1 ? __float2ll_rz(x) : __float2ll_rn(x);
+            for (int j = 0; j < 16; ++j)  // orders 0..3: x * 2^30 is an exact integer
+              run[cb * 16 + j] += oz::integral_f32_to_i64(__uint_as_float(f[j]) * two30);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)  // orders 4..6: rounded to the nearest integer
+              run[cb * 16 + j] +=
+                  oz::integral_f32_to_i64(oz::round_f32(__uint_as_float(f[j]) * two30));
           }
         }
       }

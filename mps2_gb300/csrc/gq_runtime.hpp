@@ -141,20 +141,25 @@ struct PermPlan {
   int64_t nchunks = 0;
 };
 
-// Tall-skinny contraction with a small (MPO) B operand: one pair of blocks
-// read in place through leg strides (skinny.cu).
+// Tall-skinny contraction with a small (MPO) B operand: every contributing
+// block pair read in place through leg strides (skinny.cu).  The A offsets
+// of a pair's contracted indices and the B offsets of its (k, j) values are
+// listed once at plan time.
 constexpr int kSkMaxK = 64;
+constexpr int kSkMaxFree = 4;  // free legs of A
 struct SkinnyPair {
-  int64_t a_off, b_off;
-  int K, nk, nfa, nfb;
-  int k_dims[kMaxRank];
-  int64_t ka_str[kMaxRank], kb_str[kMaxRank];
-  int fa_dims[kMaxRank];
-  int64_t fa_str[kMaxRank];
-  int fb_dims[kMaxRank];
-  int64_t fb_str[kMaxRank];
+  int64_t a_off;                // A block offset
+  int64_t fa_str[kSkMaxFree];   // A strides of the free legs, output-row order
+  int K;                        // contracted extent
+  int koff;                     // first of its K entries in the A-offset list
+  int bidx;                     // first of its K x N entries in the B-offset list
+  int pad;
 };
-struct SkinnyItem { int64_t c_off; int M, N, row0, pair_begin, pair_end; };
+struct SkinnyItem {             // one CTA: up to 256 rows of one output block
+  int64_t c_off;
+  int M, N, row0, pair_begin, pair_end, nfa;
+  int fa_dims[kSkMaxFree];
+};
 
 // Packed split-precision operand: every block as 128-row x 32-k tiles of
 // TF32 hi then lo, each tile in the tensor-core shared-memory image.
@@ -192,6 +197,8 @@ struct ContractPlan {
   bool use_skinny = false;  // small-B tall-skinny kernel (skinny.cu)
   DevArray<SkinnyItem> sk_items;
   DevArray<SkinnyPair> sk_pairs;
+  DevArray<int64_t> sk_koffs;     // A offsets of the pairs' contracted indices
+  DevArray<int> sk_bidx;          // B offsets of the pairs' (k, j) values
   int64_t sk_nitems = 0;
   int sk_jb = 8;
   bool use_tc = false;    // 3xTF32 tcgen05 kernel (else the FP64 kernel)
