@@ -255,6 +255,33 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
 }
 
 namespace {
+// Block coordinates packed 16 bits per leg (up to 8 legs), first leg most
+// significant: comparing keys compares the coordinates lexicographically.
+struct PackedKey {
+  uint64_t hi, lo;
+  bool operator<(const PackedKey &o) const { return hi != o.hi ? hi < o.hi : lo < o.lo; }
+  bool operator==(const PackedKey &o) const { return hi == o.hi && lo == o.lo; }
+};
+struct Contrib { int64_t ablk, bblk; };
+struct IntSpan {
+  const int *p;
+  size_t n;
+  const int *data() const { return p; }
+  size_t size() const { return n; }
+  int operator[](size_t i) const { return p[i]; }
+};
+struct ContribSpan {
+  const Contrib *b, *e;
+  const Contrib *begin() const { return b; }
+  const Contrib *end() const { return e; }
+  size_t size() const { return (size_t)(e - b); }
+  const Contrib &operator[](size_t i) const { return b[i]; }
+};
+struct OutGroup {  // an output block: its coordinates and its block pairs
+  IntSpan first;
+  ContribSpan second;
+};
+
 std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
                                          const std::vector<int> &axes_a,
                                          const std::vector<int> &axes_b, const Tensor *target,
@@ -292,30 +319,66 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
   pa_t.insert(pa_t.end(), free_a.begin(), free_a.end());
   pb_t.insert(pb_t.end(), axes_b.begin(), axes_b.end());
 
-  // Group B blocks by their contracted-sector key.
-  std::unordered_map<std::string, std::vector<int64_t>> bgroups;
-  std::vector<int> key(nc);
-  for (int64_t j = 0; j < b.nblocks(); ++j) {
-    const int *c = b.block_coords(j);
-    for (int i = 0; i < nc; ++i) key[i] = c[axes_b[i]];
-    bgroups[Tensor::key(key.data(), nc)].push_back(j);
-  }
-  // Output block -> contributing pairs, in (A block, B block) order.
-  struct Contrib { int64_t ablk, bblk; };
-  std::map<std::vector<int>, std::vector<Contrib>> out;
-  std::vector<int> oc(free_a.size() + free_b.size());
-  for (int64_t i = 0; i < a.nblocks(); ++i) {
-    const int *c = a.block_coords(i);
-    for (int t = 0; t < nc; ++t) key[t] = c[axes_a[t]];
-    auto it = bgroups.find(Tensor::key(key.data(), nc));
-    if (it == bgroups.end()) continue;
-    for (size_t t = 0; t < free_a.size(); ++t) oc[t] = c[free_a[t]];
-    for (int64_t j : it->second) {
-      const int *d = b.block_coords(j);
-      for (size_t t = 0; t < free_b.size(); ++t) oc[free_a.size() + t] = d[free_b[t]];
-      out[oc].push_back({i, j});
+  // Block pairs.  B blocks are grouped by their contracted-sector key; every
+  // (A block, B block) pair is tagged with its output block's coordinates
+  // packed 16 bits per leg, first leg most significant, and the pairs are
+  // sorted stably by that tag: output blocks come in ascending coordinate
+  // order, the pairs of one block in (A block, B block) order.
+  const int ro = (int)(free_a.size() + free_b.size());
+  for (const Tensor *t : {&a, &b})
+    for (const Index &ix : t->idx)
+      GQ_CHECK(ix.nsec() < 65536, "a leg with 65536 or more sectors");
+  auto pack = [](const int *c, const int *legs, int n) {
+    PackedKey k{0, 0};
+    for (int t = 0; t < n; ++t) {
+      const uint64_t v = (uint64_t)(legs ? c[legs[t]] : c[t]);
+      if (t < 4) k.hi |= v << (48 - 16 * t);
+      else k.lo |= v << (48 - 16 * (t - 4));
+    }
+    return k;
+  };
+  std::vector<std::pair<PackedKey, int64_t>> bkeys((size_t)b.nblocks());
+  for (int64_t j = 0; j < b.nblocks(); ++j) bkeys[j] = {pack(b.block_coords(j), axes_b.data(), nc), j};
+  std::stable_sort(bkeys.begin(), bkeys.end(),
+                   [](const auto &x, const auto &y) { return x.first < y.first; });
+  struct PairRec { PackedKey okey; int64_t ablk, bblk; };
+  std::vector<PairRec> prs;
+  {
+    int oc[kMaxRank];
+    for (int64_t i = 0; i < a.nblocks(); ++i) {
+      const int *c = a.block_coords(i);
+      const PackedKey k = pack(c, axes_a.data(), nc);
+      auto lo = std::lower_bound(bkeys.begin(), bkeys.end(), k,
+                                 [](const auto &x, const PackedKey &y) { return x.first < y; });
+      for (auto it = lo; it != bkeys.end() && it->first == k; ++it) {
+        const int *d = b.block_coords(it->second);
+        for (size_t t = 0; t < free_a.size(); ++t) oc[t] = c[free_a[t]];
+        for (size_t t = 0; t < free_b.size(); ++t) oc[free_a.size() + t] = d[free_b[t]];
+        prs.push_back({pack(oc, nullptr, ro), i, it->second});
+      }
     }
   }
+  std::stable_sort(prs.begin(), prs.end(),
+                   [](const PairRec &x, const PairRec &y) { return x.okey < y.okey; });
+  // Output blocks: coordinates (flat) and their pair ranges.
+  std::vector<Contrib> contribs(prs.size());
+  std::vector<int> ocoords;
+  std::vector<size_t> obeg;
+  for (size_t q = 0; q < prs.size(); ++q) {
+    contribs[q] = {prs[q].ablk, prs[q].bblk};
+    if (q == 0 || !(prs[q].okey == prs[q - 1].okey)) {
+      obeg.push_back(q);
+      const int *c = a.block_coords(prs[q].ablk), *d = b.block_coords(prs[q].bblk);
+      for (size_t t = 0; t < free_a.size(); ++t) ocoords.push_back(c[free_a[t]]);
+      for (size_t t = 0; t < free_b.size(); ++t) ocoords.push_back(d[free_b[t]]);
+    }
+  }
+  obeg.push_back(prs.size());
+  std::vector<OutGroup> out(obeg.size() - 1);
+  for (size_t g = 0; g + 1 < obeg.size(); ++g)
+    out[g] = {IntSpan{ocoords.data() + g * ro, (size_t)ro},
+              ContribSpan{contribs.data() + obeg[g], contribs.data() + obeg[g + 1]}};
+  { std::vector<PairRec>().swap(prs); }
 
   if (target) {
     GQ_CHECK(target->idx.size() == oidx.size(), "target structure has the wrong rank");
@@ -323,10 +386,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       GQ_CHECK(target->idx[l] == oidx[l], "target structure has different legs");
     plan->out = clone_structure(*target);
   } else {
-    std::vector<std::vector<int>> blocks;
-    blocks.reserve(out.size());
-    for (auto &kv : out) blocks.push_back(kv.first);
-    plan->out = make_structure(a.nq, oidx, odiv, blocks);
+    plan->out = make_structure_sorted(a.nq, oidx, odiv, ocoords);
   }
   const Tensor &o = *plan->out;
   const size_t nfa = free_a.size();
@@ -466,7 +526,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
   // part's FP64 rate, so a block goes to it when at least 2% of its padded
   // work is useful.  Tiny blocks and the MPO contractions (k and n of a few
   // units) stay on the FP64 kernel, where they are memory-bound anyway.
-  struct OutBlock { int64_t ob, m, n; const std::vector<Contrib> *pairs; bool tc; };
+  struct OutBlock { int64_t ob, m, n; const ContribSpan *pairs; bool tc; };
   std::vector<OutBlock> obs;
   obs.reserve(out.size());
   std::vector<char> touched(o.nblocks(), 0);

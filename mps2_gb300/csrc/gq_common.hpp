@@ -165,7 +165,6 @@ struct Tensor {
   QN div;
   std::vector<int> coords;        // nblocks x rank, ascending block order
   std::vector<int64_t> offs;      // nblocks + 1 prefix offsets (elements)
-  std::unordered_map<std::string, int> lut;  // coords bytes -> block id
   DevBuf data;
 
   int rank() const { return (int)idx.size(); }
@@ -175,19 +174,29 @@ struct Tensor {
   int64_t block_dim(int64_t b, int leg) const { return idx[leg].dim[block_coords(b)[leg]]; }
   int64_t block_size(int64_t b) const { return offs[b + 1] - offs[b]; }
 
-  static std::string key(const int *c, int r) {
-    return std::string(reinterpret_cast<const char *>(c), sizeof(int) * r);
-  }
+  // Block id of the coordinates c, or -1: binary search over the sorted
+  // coordinate list.
   int64_t find(const int *c) const {
-    auto it = lut.find(key(c, rank()));
-    return it == lut.end() ? -1 : it->second;
+    const int r = rank();
+    int64_t lo = 0, hi = nblocks();
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      const int *m = coords.data() + mid * r;
+      int cmp = 0;
+      for (int l = 0; l < r && cmp == 0; ++l)
+        if (m[l] != c[l]) cmp = m[l] < c[l] ? -1 : 1;
+      if (cmp == 0) return mid;
+      if (cmp < 0) lo = mid + 1;
+      else hi = mid;
+    }
+    return -1;
   }
   QN block_div(const int *c) const {
     QN q;
     for (int i = 0; i < rank(); ++i) q = q + idx[i].qn[c[i]].scaled(idx[i].dir);
     return q;
   }
-  // Build offsets and the lookup table from `coords` (must be sorted).
+  // Build the offsets from `coords` (must be sorted and unique).
   void finalize_structure();
   // Allocate device storage for the structure (contents undefined).
   void allocate();
@@ -199,6 +208,9 @@ using TensorPtr = std::shared_ptr<Tensor>;
 // Structure helpers
 TensorPtr make_structure(int nq, const std::vector<Index> &idx, const QN &div,
                          std::vector<std::vector<int>> blocks /* any order */);
+// The same from flat coordinates (nblocks x rank) already sorted and unique.
+TensorPtr make_structure_sorted(int nq, const std::vector<Index> &idx, const QN &div,
+                                std::vector<int> coords);
 // Every block allowed by `div` for these legs.
 std::vector<std::vector<int>> allowed_blocks(const std::vector<Index> &idx, const QN &div);
 TensorPtr clone_structure(const Tensor &t);

@@ -272,13 +272,10 @@ void Tensor::finalize_structure() {
   const int r = rank();
   const int64_t nb = r ? (int64_t)coords.size() / r : 1;
   offs.assign(nb + 1, 0);
-  lut.clear();
-  lut.reserve(nb * 2);
   for (int64_t b = 0; b < nb; ++b) {
     int64_t sz = 1;
     for (int l = 0; l < r; ++l) sz *= idx[l].dim[coords[b * r + l]];
     offs[b + 1] = offs[b] + sz;
-    lut.emplace(key(coords.data() + b * r, r), (int)b);
   }
 }
 
@@ -306,6 +303,17 @@ TensorPtr make_structure(int nq, const std::vector<Index> &idx, const QN &div,
     }
   }
   if (r == 0) t->coords.clear();
+  t->finalize_structure();
+  return t;
+}
+
+TensorPtr make_structure_sorted(int nq, const std::vector<Index> &idx, const QN &div,
+                                std::vector<int> coords) {
+  auto t = std::make_shared<Tensor>();
+  t->nq = nq;
+  t->idx = idx;
+  t->div = div;
+  t->coords = std::move(coords);
   t->finalize_structure();
   return t;
 }
@@ -344,7 +352,6 @@ TensorPtr clone_structure(const Tensor &t) {
   o->div = t.div;
   o->coords = t.coords;
   o->offs = t.offs;
-  o->lut = t.lut;
   return o;
 }
 
