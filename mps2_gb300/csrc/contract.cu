@@ -232,6 +232,7 @@ std::shared_ptr<ContractPlan> plan_contract(const Tensor &a, const Tensor &b,
   f.add(target ? 1 : 0);
   if (target) f.add_tensor(*target);
   f.add((uint64_t)prec);
+  f.add(autotune_on() ? 1 : 0);  // plans carry the autotuner key only when it is on
   uint64_t fb;
   std::memcpy(&fb, &tc_frac, sizeof(fb));
   f.add(fb);
@@ -439,6 +440,52 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
         }
       };
       const int nfree = (int)free_a.size();
+      // The A offsets of the contracted indices depend on the A block only,
+      // the B offsets of the (k, j) values on the B block only: listed once
+      // per block, shared by its pairs.
+      std::vector<int> a_list(a.nblocks(), -1), b_list(b.nblocks(), -1);
+      auto a_offsets = [&](int64_t ablk, const int64_t *sa, int K) {
+        if (a_list[ablk] < 0) {
+          a_list[ablk] = (int)koffs.size();
+          for (int e = 0; e < K; ++e) {  // last contracted leg fastest
+            int rem = e;
+            int64_t oa = 0;
+            for (int t = nc - 1; t >= 0; --t) {
+              const int d = (int)a.block_dim(ablk, axes_a[t]);
+              oa += (int64_t)(rem % d) * sa[axes_a[t]];
+              rem /= d;
+            }
+            koffs.push_back(oa);
+          }
+        }
+        return a_list[ablk];
+      };
+      auto b_offsets = [&](int64_t bblk, int K, int64_t n) {
+        if (b_list[bblk] < 0) {
+          int64_t sb[kMaxRank];
+          strides(b, bblk, sb);
+          b_list[bblk] = (int)bidx.size();
+          for (int e = 0; e < K; ++e) {  // j over B's free legs, last fastest
+            int rem = e;
+            int64_t obk = b.offs[bblk];
+            for (int t = nc - 1; t >= 0; --t) {
+              const int d = (int)b.block_dim(bblk, axes_b[t]);
+              obk += (int64_t)(rem % d) * sb[axes_b[t]];
+              rem /= d;
+            }
+            for (int64_t j = 0; j < n; ++j) {
+              int64_t rj = j, o2 = obk;
+              for (int t = (int)free_b.size() - 1; t >= 0; --t) {
+                const int64_t d = b.block_dim(bblk, free_b[t]);
+                o2 += (rj % d) * sb[free_b[t]];
+                rj /= d;
+              }
+              bidx.push_back((int)o2);
+            }
+          }
+        }
+        return b_list[bblk];
+      };
       for (auto &kv : out) {
         const int64_t ob = o.find(kv.first.data());
         GQ_CHECK(ob >= 0, "contraction produces a block missing from the target structure");
@@ -449,9 +496,8 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
         const int pb = (int)sp.size();
         int fdims[kSkMaxFree] = {1, 1, 1, 1};
         for (auto &cp : kv.second) {
-          int64_t sa[kMaxRank], sb[kMaxRank];
+          int64_t sa[kMaxRank];
           strides(a, cp.ablk, sa);
-          strides(b, cp.bblk, sb);
           SkinnyPair q{};
           q.a_off = a.offs[cp.ablk];
           q.K = 1;
@@ -460,38 +506,8 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
             fdims[t] = (int)a.block_dim(cp.ablk, free_a[t]);
             q.fa_str[t] = sa[free_a[t]];
           }
-          // A offsets of the contracted indices, last contracted leg fastest
-          q.koff = (int)koffs.size();
-          for (int e = 0; e < q.K; ++e) {
-            int rem = e;
-            int64_t oa = 0;
-            for (int t = nc - 1; t >= 0; --t) {
-              const int d = (int)a.block_dim(cp.ablk, axes_a[t]);
-              oa += (int64_t)(rem % d) * sa[axes_a[t]];
-              rem /= d;
-            }
-            koffs.push_back(oa);
-          }
-          // B offsets of the (k, j) values, j over B's free legs (last fastest)
-          q.bidx = (int)bidx.size();
-          for (int e = 0; e < q.K; ++e) {
-            int rem = e;
-            int64_t obk = b.offs[cp.bblk];
-            for (int t = nc - 1; t >= 0; --t) {
-              const int d = (int)b.block_dim(cp.bblk, axes_b[t]);
-              obk += (int64_t)(rem % d) * sb[axes_b[t]];
-              rem /= d;
-            }
-            for (int64_t j = 0; j < n; ++j) {
-              int64_t rj = j, o2 = obk;
-              for (int t = (int)free_b.size() - 1; t >= 0; --t) {
-                const int64_t d = b.block_dim(cp.bblk, free_b[t]);
-                o2 += (rj % d) * sb[free_b[t]];
-                rj /= d;
-              }
-              bidx.push_back((int)o2);
-            }
-          }
+          q.koff = a_offsets(cp.ablk, sa, q.K);
+          q.bidx = b_offsets(cp.bblk, q.K, n);
           sp.push_back(q);
           plan->flops += 2.0 * (double)m * (double)n * (double)q.K;
         }
@@ -574,8 +590,9 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
     obs.push_back({ob, m, n, &kv.second, tc});
   }
   // autotuner key: the 16 heaviest output blocks' (log2 m, log2 n, log2 k of
-  // their largest pair) and log2 of the block count, hashed (FNV-1a)
-  {
+  // their largest pair) and log2 of the block count, hashed (FNV-1a); only
+  // the autotuner reads it
+  if (autotune_on()) {
     std::vector<std::array<int, 4>> h;
     for (auto &b0 : obs) {
       int64_t kmax = 1;

