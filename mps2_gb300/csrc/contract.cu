@@ -35,9 +35,13 @@ bool is_identity(const std::vector<int> &p) {
   return true;
 }
 
-void build_perm_plan(const Tensor &t, const std::vector<int> &perm, PermPlan &pp) {
+// Permute the blocks with used[b] != 0 (all if used is null) into the same
+// offsets of the destination buffer.
+void build_perm_plan(const Tensor &t, const std::vector<int> &perm, PermPlan &pp,
+                     const std::vector<char> *used = nullptr) {
   pp.needed = true;
   pp.total = t.size();
+  pp.moved = 0;
   const int r = t.rank();
   std::vector<PermBlock> blocks;
   std::vector<PermChunk> chunks;
@@ -60,6 +64,8 @@ void build_perm_plan(const Tensor &t, const std::vector<int> &perm, PermPlan &pp
       pb.sstride[j] = sstr[perm[j]];
     }
     blocks.push_back(pb);
+    if (used && !(*used)[b]) continue;
+    pp.moved += pb.n;
     for (int64_t e = 0; e < pb.n; e += kPermChunk)
       chunks.push_back({(int)b, e, std::min<int64_t>(pb.n, e + kPermChunk)});
   }
@@ -94,7 +100,7 @@ void run_perm(const PermPlan &pp, const double *src, double *dst) {
   permute_blocks_kernel<<<(unsigned)pp.nchunks, 256, 0, stream()>>>(pp.blocks.p, pp.chunks.p, src,
                                                                       dst);
   GQ_CUDA(cudaGetLastError());
-  prof_end(kProfPermute, 0.0, 16.0 * (double)pp.total);
+  prof_end(kProfPermute, 0.0, 16.0 * (double)pp.moved);
 }
 
 }  // namespace
@@ -424,20 +430,21 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       std::vector<int> bidx;
       std::vector<char> touched(o.nblocks(), 0);
       const int rows = skinny_rows_per_cta();
+      int64_t nctas = 0;
       auto add_items = [&](int64_t c_off, int64_t m, int64_t n, int pb, int pe,
                            const int *fdims, int nf) {
-        for (int64_t r0 = 0; r0 < m; r0 += rows) {
-          SkinnyItem it{};
-          it.c_off = c_off;
-          it.M = (int)m;
-          it.N = (int)n;
-          it.row0 = (int)r0;
-          it.pair_begin = pb;
-          it.pair_end = pe;
-          it.nfa = nf;
-          for (int t = 0; t < kSkMaxFree; ++t) it.fa_dims[t] = t < nf ? fdims[t] : 1;
-          items.push_back(it);
-        }
+        if (m == 0 || n == 0) return;
+        SkinnyItem it{};
+        it.c_off = c_off;
+        it.M = (int)m;
+        it.N = (int)n;
+        it.cta0 = (int)nctas;
+        it.pair_begin = pb;
+        it.pair_end = pe;
+        it.nfa = nf;
+        for (int t = 0; t < kSkMaxFree; ++t) it.fa_dims[t] = t < nf ? fdims[t] : 1;
+        items.push_back(it);
+        nctas += (m + rows - 1) / rows;
       };
       const int nfree = (int)free_a.size();
       // The A offsets of the contracted indices depend on the A block only,
@@ -526,7 +533,9 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       }
       plan->use_skinny = true;
       plan->sk_jb = max_n <= 2 ? 2 : max_n <= 4 ? 4 : max_n <= 8 ? 8 : max_n <= 16 ? 16 : 32;
+      GQ_CHECK(nctas < (int64_t(1) << 31), "tall-skinny launch too large");
       plan->sk_nitems = (int64_t)items.size();
+      plan->sk_nctas = nctas;
       plan->sk_items.upload(items);
       plan->sk_pairs.upload(sp);
       plan->sk_koffs.upload(koffs);
@@ -537,16 +546,28 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
     }
   }
 
-  // Per output block kernel choice.  The tensor-core form pads every block
-  // to 128 x 128 x 32 tiles; its TF32 rate is a few hundred times this
-  // part's FP64 rate, so a block goes to it when at least 2% of its padded
-  // work is useful.  Tiny blocks and the MPO contractions (k and n of a few
-  // units) stay on the FP64 kernel, where they are memory-bound anyway.
-  struct OutBlock { int64_t ob, m, n; const ContribSpan *pairs; bool tc; };
+  // Per output block kernel choice: the FP64 tiles (64 x 64), 3xTF32 tiles
+  // (128 x 128) or FP64-accurate tiles (128 x 96), each padding a block to
+  // whole tiles (k to multiples of 32 on the tensor cores).
+  //  * The form's own tensor-core kernel takes a block when at least 2%
+  //    (3xTF32) or 3% (FP64-accurate) of its padded work is useful: those
+  //    rates are a few hundred and ~35 times this part's FP64 rate.
+  //  * Otherwise, by default, a block goes to the FP64-accurate kernel when
+  //    its padded work there costs less time than the FP64 kernel's padded
+  //    tiles: thin blocks (a few rows or columns, long k) waste most of
+  //    either tile and the FP64 pipe of this part is ~20x slower.  In the
+  //    split form too: there the thin blocks keep FP64 accuracy (moved to
+  //    3xTF32 they shift its Lanczos convergence enough to leave the
+  //    per-sweep energy parity of 1e-9).
+  //  * The rest -- tiny blocks and MPO contractions -- stays on the FP64
+  //    kernel, where it is memory-bound anyway.  The FP64-accurate kernel's
+  //    exact running sums cover k <= oz_max_k().
+  enum Kind : int { kKindFp64 = 0, kKindTf32 = 1, kKindOz = 2 };
+  struct OutBlock { int64_t ob, m, n; const ContribSpan *pairs; int kind; };
   std::vector<OutBlock> obs;
   obs.reserve(out.size());
   std::vector<char> touched(o.nblocks(), 0);
-  bool any_tc = false, any_fp = false;
+  bool any_tf32 = false, any_oz = false, any_fp = false;
   for (auto &kv : out) {
     const int64_t ob = o.find(kv.first.data());
     GQ_CHECK(ob >= 0, "contraction produces a block missing from the target structure");
@@ -554,40 +575,37 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
     int64_t m = 1, n = 1;
     for (size_t l = 0; l < nfa; ++l) m *= o.idx[l].dim[kv.first[l]];
     for (size_t l = nfa; l < kv.first.size(); ++l) n *= o.idx[l].dim[kv.first[l]];
-    bool tc = false;
+    int kind = kKindFp64;
     if (prec == kTF32x3 || prec == kFP64TC) {
-      // FP64-accurate form: 128 x 96 tiles, about 35 times the FP64 rate
       const int TM = prec == kTF32x3 ? 128 : oz_tile_m();
       const int TN = prec == kTF32x3 ? 128 : oz_tile_n();
+      const int OM = oz_tile_m(), ON = oz_tile_n();
       const double frac = tc_frac >= 0.0 ? tc_frac : (prec == kTF32x3 ? 0.02 : 0.03);
       plan->tc_frac = frac;
-      double useful = 0.0, padded = 0.0, padded_fp64 = 0.0;
+      double useful = 0.0, padded = 0.0, padded_oz = 0.0, padded_fp64 = 0.0;
       int64_t ksum = 0;
       for (auto &cp : kv.second) {
         int64_t k = 1;
         for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
+        const double kp = (k + 31) / 32 * 32.0;
         useful += 2.0 * m * n * k;
-        padded += 2.0 * (double)((m + TM - 1) / TM * TM) * (double)((n + TN - 1) / TN * TN) *
-                  ((k + 31) / 32 * 32.0);
+        padded += 2.0 * (double)((m + TM - 1) / TM * TM) * (double)((n + TN - 1) / TN * TN) * kp;
+        padded_oz += 2.0 * (double)((m + OM - 1) / OM * OM) * (double)((n + ON - 1) / ON * ON) * kp;
         padded_fp64 += 2.0 * (double)((m + 63) / 64 * 64) * (double)((n + 63) / 64 * 64) * k;
         ksum += (k + 31) / 32 * 32;
       }
-      tc = useful >= frac * padded;
-      // In the FP64-accurate form a block also goes to the tensor cores by
-      // default when their padded work costs less time than the FP64
-      // kernel's padded 64 x 64 tiles: thin blocks (a few rows or columns,
-      // long k) waste most of either tile, and the FP64 pipe of this part is
-      // ~20x slower than that form.  (The split form keeps thin blocks in
-      // FP64: moved to 3xTF32 they shift its Lanczos convergence enough to
-      // leave the per-sweep energy parity of 1e-9 on transient sweeps.)
-      if (prec == kFP64TC && tc_frac < 0.0 && padded < 20.0 * padded_fp64) tc = true;
-      // the FP64-accurate kernel's exact running sums cover k <= oz_max_k()
-      if (prec == kFP64TC && ksum > oz_max_k()) tc = false;
-      if (tc) plan->padded_flops += padded;
+      const bool oz_ok = ksum <= oz_max_k();
+      if (useful >= frac * padded && (prec == kTF32x3 || oz_ok))
+        kind = prec == kTF32x3 ? kKindTf32 : kKindOz;
+      else if (tc_frac < 0.0 && oz_ok && padded_oz < 20.0 * padded_fp64)
+        kind = kKindOz;
+      if (kind == kKindTf32) plan->padded_flops += padded;
+      if (kind == kKindOz) plan->padded_flops += padded_oz;
     }
-    any_tc |= tc;
-    any_fp |= !tc;
-    obs.push_back({ob, m, n, &kv.second, tc});
+    any_tf32 |= kind == kKindTf32;
+    any_oz |= kind == kKindOz;
+    any_fp |= kind == kKindFp64;
+    obs.push_back({ob, m, n, &kv.second, kind});
   }
   // autotuner key: the 16 heaviest output blocks' (log2 m, log2 n, log2 k of
   // their largest pair) and log2 of the block count, hashed (FNV-1a); only
@@ -620,16 +638,28 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
   for (int64_t ob = 0; ob < o.nblocks(); ++ob)
     if (!touched[ob]) { any_fp = true; plan->nzero_blocks++; }
 
-  const bool oz = prec == kFP64TC;
-  plan->use_tc = any_tc && !oz;
-  plan->use_oz = any_tc && oz;
+  plan->use_tc = any_tf32;
+  plan->use_oz = any_oz;
+  // operand blocks read by each kernel's tiles: each pack or permute covers
+  // only its own
+  std::vector<char> a_use[3], b_use[3];
+  for (int k = 0; k < 3; ++k) {
+    a_use[k].assign(a.nblocks(), 0);
+    b_use[k].assign(b.nblocks(), 0);
+  }
+  for (auto &b0 : obs)
+    for (auto &cp : *b0.pairs) {
+      a_use[b0.kind][cp.ablk] = 1;
+      b_use[b0.kind][cp.bblk] = 1;
+    }
+  std::vector<char> &a_fp = a_use[kKindFp64], &b_fp = b_use[kKindFp64];
   if (plan->use_tc) {
-    build_tc_pack(a, free_a, axes_a, plan->ta);
-    build_tc_pack(b, free_b, axes_b, plan->tb);
+    build_tc_pack(a, free_a, axes_a, plan->ta, &a_use[kKindTf32]);
+    build_tc_pack(b, free_b, axes_b, plan->tb, &b_use[kKindTf32]);
   }
   if (plan->use_oz) {
-    build_oz_pack(a, free_a, axes_a, oz_tile_m(), plan->oa);
-    build_oz_pack(b, free_b, axes_b, oz_tile_n(), plan->ob);
+    build_oz_pack(a, free_a, axes_a, oz_tile_m(), plan->oa, &a_use[kKindOz]);
+    build_oz_pack(b, free_b, axes_b, oz_tile_n(), plan->ob, &b_use[kKindOz]);
   }
   if (any_fp) {
     if (is_identity(pa)) {
@@ -638,7 +668,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       plan->transA = 1;
     } else {
       plan->transA = 0;
-      build_perm_plan(a, pa, plan->pa);
+      build_perm_plan(a, pa, plan->pa, &a_fp);
     }
     if (is_identity(pb)) {
       plan->transB = 0;
@@ -646,7 +676,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       plan->transB = 1;
     } else {
       plan->transB = 0;
-      build_perm_plan(b, pb, plan->pb);
+      build_perm_plan(b, pb, plan->pb, &b_fp);
     }
   }
 
@@ -671,7 +701,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       }
   };
   for (auto &b0 : obs) {
-    if (b0.tc && oz) {
+    if (b0.kind == kKindOz) {
       const int pbeg = (int)pairs_oz.size();
       int64_t ksum = 0;
       for (auto &cp : *b0.pairs) {
@@ -703,15 +733,16 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
         }
       continue;
     }
-    auto &pl = b0.tc ? pairs_tc : pairs;
+    const bool tc = b0.kind == kKindTf32;
+    auto &pl = tc ? pairs_tc : pairs;
     const int pbeg = (int)pl.size();
     int64_t ksum = 0;
     for (auto &cp : *b0.pairs) {
       int64_t k = 1;
       for (int t = 0; t < nc; ++t) k *= a.block_dim(cp.ablk, axes_a[t]);
       GemmPair gp{};
-      gp.a_off = b0.tc ? plan->ta.base[cp.ablk] : a.offs[cp.ablk];
-      gp.b_off = b0.tc ? plan->tb.base[cp.bblk] : b.offs[cp.bblk];
+      gp.a_off = tc ? plan->ta.base[cp.ablk] : a.offs[cp.ablk];
+      gp.b_off = tc ? plan->tb.base[cp.bblk] : b.offs[cp.bblk];
       gp.k = (int)k;
       gp.lda = (int)(plan->transA ? b0.m : k);
       gp.ldb = (int)(plan->transB ? k : b0.n);
@@ -719,9 +750,9 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       ksum += k;
       const double f = 2.0 * (double)b0.m * (double)b0.n * (double)k;
       plan->flops += f;
-      if (b0.tc) plan->flops_tc += f;
+      if (tc) plan->flops_tc += f;
     }
-    if (b0.tc)
+    if (tc)
       add_tiles(tiles_tc, o.offs[b0.ob], b0.m, b0.n, pbeg, (int)pl.size(), ksum,
                 gemm_tile_m(kTF32x3), gemm_tile_n(kTF32x3));
     else
@@ -745,8 +776,8 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
   plan->ntiles_oz = (int64_t)tiles_oz.size();
   plan->tiles_oz.upload(tiles_oz);
   plan->pairs_oz.upload(pairs_oz);
-  plan->tile_m = gemm_tile_m(any_tc ? kTF32x3 : kFP64);
-  plan->tile_n = gemm_tile_n(any_tc ? kTF32x3 : kFP64);
+  plan->tile_m = gemm_tile_m(any_tf32 ? kTF32x3 : kFP64);
+  plan->tile_n = gemm_tile_n(any_tf32 ? kTF32x3 : kFP64);
   plan->ntiles = (int64_t)tiles.size();
   plan->tiles.upload(tiles);
   plan->pairs.upload(pairs);
@@ -789,7 +820,6 @@ void cache_operand(ContractPlan &p, int which, const double *src) {
       run_oz_pack(p.ob, src, oz_layout(p.ob, p.b_oz.p));
       p.b_oz_cached = true;
     }
-    return;
   }
   if (!p.use_tc) return;
   if (which == 0) {

@@ -543,7 +543,8 @@ int oz_tile_n() { return oz::BN; }
 int64_t oz_max_k() { return oz::kMaxK; }
 
 void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
-                   const std::vector<int> &k_legs, int tile_rows, OzPackPlan &pp) {
+                   const std::vector<int> &k_legs, int tile_rows, OzPackPlan &pp,
+                   const std::vector<char> *used) {
   std::vector<OzPackBlock> blocks;
   std::vector<OzPackTask> tasks;
   pp.base.assign(t.nblocks(), 0);
@@ -564,8 +565,15 @@ void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
   int nrows = 0;
   int64_t off = 0;
   const int r = t.rank();
+  blocks.reserve(t.nblocks());
   for (int64_t b = 0; b < t.nblocks(); ++b) {
     OzPackBlock pb{};
+    if (used && !(*used)[b]) {  // no image: keep the entry, no rows, no tasks
+      pb.dst_off = off;
+      pp.base[b] = off;
+      blocks.push_back(pb);
+      continue;
+    }
     int64_t str[kMaxRank];
     int64_t s = 1;
     for (int l = r - 1; l >= 0; --l) {

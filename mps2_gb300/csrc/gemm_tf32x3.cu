@@ -480,14 +480,21 @@ PackBlock pack_block(const Tensor &t, int64_t b, const std::vector<int> &rl,
 }  // namespace
 
 void build_tc_pack(const Tensor &t, const std::vector<int> &row_legs,
-                   const std::vector<int> &k_legs, TcPackPlan &pp) {
+                   const std::vector<int> &k_legs, TcPackPlan &pp,
+                   const std::vector<char> *used) {
   std::vector<PackBlock> blocks;
   std::vector<PackTask> tasks;
   pp.base.assign(t.nblocks(), 0);
+  blocks.reserve(t.nblocks());
   int64_t off = 0;
   for (int64_t b = 0; b < t.nblocks(); ++b) {
     PackBlock pb = pack_block(t, b, row_legs, k_legs, off);
     pp.base[b] = off;
+    if (used && !(*used)[b]) {  // no image: keep the entry, no space, no tasks
+      pb.nrt = pb.nkt = 0;
+      blocks.push_back(pb);
+      continue;
+    }
     off += (int64_t)pb.nrt * pb.nkt * 2 * tc::kTileFloats;
     for (int rt = 0; rt < pb.nrt; ++rt)
       for (int kt = 0; kt < pb.nkt; ++kt) tasks.push_back({(int)b, rt, kt});

@@ -135,7 +135,8 @@ struct PermChunk { int block; int64_t begin, end; };
 
 struct PermPlan {
   bool needed = false;
-  int64_t total = 0;
+  int64_t total = 0;   // elements of the destination layout
+  int64_t moved = 0;   // elements actually permuted
   DevArray<PermBlock> blocks;
   DevArray<PermChunk> chunks;
   int64_t nchunks = 0;
@@ -155,9 +156,9 @@ struct SkinnyPair {
   int bidx;                     // first of its K x N entries in the B-offset list
   int pad;
 };
-struct SkinnyItem {             // one CTA: up to 256 rows of one output block
+struct SkinnyItem {             // one output block, cut into CTAs of 256 rows
   int64_t c_off;
-  int M, N, row0, pair_begin, pair_end, nfa;
+  int M, N, cta0, pair_begin, pair_end, nfa;  // cta0: its first CTA
   int fa_dims[kSkMaxFree];
 };
 
@@ -199,7 +200,8 @@ struct ContractPlan {
   DevArray<SkinnyPair> sk_pairs;
   DevArray<int64_t> sk_koffs;     // A offsets of the pairs' contracted indices
   DevArray<int> sk_bidx;          // B offsets of the pairs' (k, j) values
-  int64_t sk_nitems = 0;
+  int64_t sk_nitems = 0;   // output blocks
+  int64_t sk_nctas = 0;    // CTAs of the launch
   int sk_jb = 8;
   bool use_tc = false;    // 3xTF32 tcgen05 kernel (else the FP64 kernel)
   TcPackPlan ta, tb;
@@ -280,8 +282,11 @@ int skinny_rows_per_cta();
 // GEMM kernels (launched by run_contract)
 void launch_gemm_fp64(const ContractPlan &p, const double *A, const double *B, double *C);
 void launch_gemm_tf32x3(const ContractPlan &p, const float *A, const float *B, double *C);
+// The pack plans cover the blocks with used[b] != 0 (every block if used is
+// null); the other blocks get no packed image.
 void build_oz_pack(const Tensor &t, const std::vector<int> &row_legs,
-                   const std::vector<int> &k_legs, int tile_rows, OzPackPlan &pp);
+                   const std::vector<int> &k_legs, int tile_rows, OzPackPlan &pp,
+                   const std::vector<char> *used = nullptr);
 int64_t oz_pack_doubles(const OzPackPlan &pp);
 OzPacked oz_layout(const OzPackPlan &pp, double *buf);
 void run_oz_pack(const OzPackPlan &pp, const double *src, const OzPacked &dst);
@@ -290,7 +295,8 @@ int oz_tile_m();
 int oz_tile_n();
 int64_t oz_max_k();  // k of one FP64-accurate output tile, summed over its pairs
 void build_tc_pack(const Tensor &t, const std::vector<int> &row_legs,
-                   const std::vector<int> &k_legs, TcPackPlan &pp);
+                   const std::vector<int> &k_legs, TcPackPlan &pp,
+                   const std::vector<char> *used = nullptr);
 void run_tc_pack(const TcPackPlan &pp, const double *src, float *dst);
 int gemm_tile_m(Precision prec);
 int gemm_tile_n(Precision prec);

@@ -33,14 +33,23 @@ constexpr int kSkPool = 4096;   // output staging (doubles)
 
 template <int JB>
 __global__ void __launch_bounds__(kSkRows)
-    skinny_kernel(const SkinnyItem *__restrict__ items, const SkinnyPair *__restrict__ pairs,
+    skinny_kernel(const SkinnyItem *__restrict__ items, int nitems,
+                  const SkinnyPair *__restrict__ pairs,
                   const int64_t *__restrict__ koffs, const int *__restrict__ bidx,
                   const double *__restrict__ A, const double *__restrict__ B,
                   double *__restrict__ C) {
   __shared__ double pool[kSkPool];
-  const SkinnyItem it = items[blockIdx.x];
+  // this CTA's output block: the last item whose first CTA is <= blockIdx.x
+  int lo = 0, hi = nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (items[mid].cta0 <= (int)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const SkinnyItem it = items[lo];
+  const int row0 = ((int)blockIdx.x - it.cta0) * kSkRows;
   const int tid = threadIdx.x;
-  const int i = it.row0 + tid;
+  const int i = row0 + tid;
   const bool live = i < it.M;
   // the row's coordinates along A's free legs
   int fc[kSkMaxFree];
@@ -79,7 +88,7 @@ __global__ void __launch_bounds__(kSkRows)
         }
       }
     }
-    const int nrows = min(kSkRows, it.M - it.row0);
+    const int nrows = min(kSkRows, it.M - row0);
     if (jn == N) {
       // one pass holds every column: the CTA's rows are one contiguous
       // stretch of C, written through shared memory in full lines
@@ -92,7 +101,7 @@ __global__ void __launch_bounds__(kSkRows)
             if (j < jn) pool[(tid - r0) * N + j] = acc[j];
         }
         __syncthreads();
-        double *c = C + it.c_off + (int64_t)(it.row0 + r0) * N;
+        double *c = C + it.c_off + (int64_t)(row0 + r0) * N;
         for (int e = tid; e < rn * N; e += kSkRows) c[e] = pool[e];
         __syncthreads();
       }
@@ -120,24 +129,25 @@ void launch_skinny(const ContractPlan &p, const double *A, const double *B, doub
   if (p.sk_nitems == 0) return;
   prof_begin(kProfSkinny);
   auto s = stream();
-  const unsigned grid = (unsigned)p.sk_nitems;
+  const unsigned grid = (unsigned)p.sk_nctas;
+  const int ni = (int)p.sk_nitems;
   const int64_t *ko = p.sk_koffs.p;
   const int *bi = p.sk_bidx.p;
   switch (p.sk_jb) {
     case 2:
-      skinny_kernel<2><<<grid, kSkRows, 0, s>>>(p.sk_items.p, p.sk_pairs.p, ko, bi, A, B, C);
+      skinny_kernel<2><<<grid, kSkRows, 0, s>>>(p.sk_items.p, ni, p.sk_pairs.p, ko, bi, A, B, C);
       break;
     case 4:
-      skinny_kernel<4><<<grid, kSkRows, 0, s>>>(p.sk_items.p, p.sk_pairs.p, ko, bi, A, B, C);
+      skinny_kernel<4><<<grid, kSkRows, 0, s>>>(p.sk_items.p, ni, p.sk_pairs.p, ko, bi, A, B, C);
       break;
     case 8:
-      skinny_kernel<8><<<grid, kSkRows, 0, s>>>(p.sk_items.p, p.sk_pairs.p, ko, bi, A, B, C);
+      skinny_kernel<8><<<grid, kSkRows, 0, s>>>(p.sk_items.p, ni, p.sk_pairs.p, ko, bi, A, B, C);
       break;
     case 16:
-      skinny_kernel<16><<<grid, kSkRows, 0, s>>>(p.sk_items.p, p.sk_pairs.p, ko, bi, A, B, C);
+      skinny_kernel<16><<<grid, kSkRows, 0, s>>>(p.sk_items.p, ni, p.sk_pairs.p, ko, bi, A, B, C);
       break;
     default:
-      skinny_kernel<32><<<grid, kSkRows, 0, s>>>(p.sk_items.p, p.sk_pairs.p, ko, bi, A, B, C);
+      skinny_kernel<32><<<grid, kSkRows, 0, s>>>(p.sk_items.p, ni, p.sk_pairs.p, ko, bi, A, B, C);
   }
   GQ_CUDA(cudaGetLastError());
   prof_end(kProfSkinny, p.flops, 8.0 * (double)(p.a_elems + p.b_elems + p.out->size()));
