@@ -23,7 +23,8 @@
 //  * new bond sectors: groups with a kept value, ascending charge.
 //
 // Decomposition routes (all FP64):
-//  * groups with m, n <= 32: one batched Jacobi SVD for all of them;
+//  * groups with m, n <= 32: one-sided Jacobi SVD, one CTA per group
+//    (small_svd_kernel);
 //  * larger groups inside a sweep update: only the factor that becomes the
 //    canonical MPS tensor has to be orthonormal, so it is taken from the
 //    eigenvectors of the Gram matrix on that side and the other factor comes
@@ -141,6 +142,117 @@ __global__ void pad_small_kernel(const PadItem *__restrict__ items, const double
     const int r = e % kSmall, c = e / kSmall;
     dst[it.dst_off + e] = (r < it.n && c < it.m) ? src[it.src_off + r + (int64_t)c * it.n] : 0.0;
   }
+}
+
+// One-sided (Hestenes) Jacobi SVD of every 32 x 32 slot X (column-major),
+// one CTA per slot: the columns are rotated in pairs -- 16 disjoint pairs
+// per round in round-robin order, one warp per pair, a lane per row --
+// until a sweep rotates no pair (|x_p . x_q| <= 1e-15 |x_p| |x_q| for every
+// pair, or one of the two columns below 1e-15 of |X|_F: rounding noise left
+// by a rank-deficient X, which would otherwise keep rotating) or after
+// kSmallSweeps sweeps.  Then X V = W has orthogonal columns:
+// sigma_j = |w_j| and u_j = w_j / sigma_j (zero where sigma_j = 0).  Output
+// in the layout of the batched library solve it replaces: sigma descending
+// (ties: lower column first), U and V column-major 32 x 32.
+constexpr int kSmallSweeps = 60;
+constexpr double kSmallJacobiTol = 1e-15;
+
+__device__ __forceinline__ double warp_sum_all(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Column at position j of round `round` of the round-robin pairing of 32
+// columns (position 0 fixed, the other 31 rotating).
+__device__ __forceinline__ int rr_column(int j, int round) {
+  return j == 0 ? 0 : (j - 1 + round) % (kSmall - 1) + 1;
+}
+
+__global__ void __launch_bounds__(256)
+    small_svd_kernel(const double *__restrict__ X, double *__restrict__ U,
+                     double *__restrict__ V, double *__restrict__ S) {
+  __shared__ double w[kSmall][kSmall + 1];  // w[column][row]
+  __shared__ double v[kSmall][kSmall + 1];
+  __shared__ double sig[kSmall];
+  __shared__ int perm[kSmall];
+  __shared__ int rot[2];
+  __shared__ double negligible;
+  const int64_t base = (int64_t)blockIdx.x * kSmall * kSmall;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int e = threadIdx.x; e < kSmall * kSmall; e += blockDim.x) {
+    const int r = e % kSmall, c = e / kSmall;
+    w[c][r] = X[base + e];
+    v[c][r] = r == c ? 1.0 : 0.0;
+  }
+  if (threadIdx.x == 0) rot[0] = rot[1] = 0;
+  __syncthreads();
+  for (int c = warp; c < kSmall; c += nwarps) {
+    const double x = w[c][lane];
+    const double n2 = warp_sum_all(x * x);
+    if (lane == 0) sig[c] = n2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double f2 = 0.0;
+    for (int c = 0; c < kSmall; ++c) f2 += sig[c];
+    negligible = 1e-30 * f2;  // (1e-15 |X|_F)^2
+  }
+  __syncthreads();
+  const double neg = negligible;
+  for (int sweep = 0; sweep < kSmallSweeps; ++sweep) {
+    int mine = 0;
+    for (int round = 0; round < kSmall - 1; ++round) {
+      for (int pi = warp; pi < kSmall / 2; pi += nwarps) {
+        const int p = rr_column(pi, round), q = rr_column(kSmall - 1 - pi, round);
+        const double a = w[p][lane], b = w[q][lane];
+        const double alpha = warp_sum_all(a * a), beta = warp_sum_all(b * b);
+        const double gamma = warp_sum_all(a * b);
+        if (gamma != 0.0 && fabs(gamma) > kSmallJacobiTol * sqrt(alpha * beta) &&
+            fmin(alpha, beta) > neg) {
+          const double zeta = (beta - alpha) / (2.0 * gamma);
+          const double t = fabs(zeta) > 1e150
+                               ? 0.5 / zeta
+                               : (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+          w[p][lane] = c * a - sn * b;
+          w[q][lane] = sn * a + c * b;
+          const double vp = v[p][lane], vq = v[q][lane];
+          v[p][lane] = c * vp - sn * vq;
+          v[q][lane] = sn * vp + c * vq;
+          mine = 1;
+        }
+      }
+      __syncthreads();
+    }
+    if (mine && lane == 0) atomicOr(&rot[sweep & 1], 1);
+    __syncthreads();
+    const int any = rot[sweep & 1];
+    if (threadIdx.x == 0) rot[(sweep + 1) & 1] = 0;
+    if (!any) break;
+  }
+  for (int c = warp; c < kSmall; c += nwarps) {
+    const double x = w[c][lane];
+    const double n2 = warp_sum_all(x * x);
+    if (lane == 0) sig[c] = sqrt(n2);
+  }
+  __syncthreads();
+  if (threadIdx.x < kSmall) {
+    const int c = threadIdx.x;
+    int rank = 0;
+    for (int j = 0; j < kSmall; ++j)
+      if (sig[j] > sig[c] || (sig[j] == sig[c] && j < c)) ++rank;
+    perm[rank] = c;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kSmall * kSmall; e += blockDim.x) {
+    const int r = e % kSmall, j = e / kSmall;
+    const int c = perm[j];
+    const double sc = sig[c];
+    U[base + e] = sc > 0.0 ? w[c][r] / sc : 0.0;
+    V[base + e] = v[c][r];
+  }
+  if (threadIdx.x < kSmall) S[(int64_t)blockIdx.x * kSmall + threadIdx.x] = sig[perm[threadIdx.x]];
 }
 
 // Gram slot set-up: outside the leading dim x dim block, -1 on the diagonal
@@ -481,25 +593,17 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   } jinfo_guard;
   GQ_SOLVER(cusolverDnCreateGesvdjInfo(&jinfo_guard.p));
   gesvdjInfo_t prm = jinfo_guard.p;
-  // small groups: one batched Jacobi SVD on zero-padded 32 x 32 slots of X
+  // small groups: one-sided Jacobi SVD on zero-padded 32 x 32 slots of X
   const int64_t slot = kSmall * kSmall;
   DevBuf sbatch(n_small * slot), su(n_small * slot), sv(n_small * slot), ss(n_small * kSmall);
-  DevArray<int> sinfo;
   if (n_small > 0) {
     std::vector<PadItem> items;
     for (Group *g : groups)
       if (g->route == kSmallJacobi)
         items.push_back({g->mat_off, g->small_idx * slot, (int)g->n, (int)g->m});
     launch_items(pad_small_kernel, items, mats.p, sbatch.p);
-    int lw = 0;
-    GQ_SOLVER(cusolverDnDgesvdjBatched_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, kSmall, kSmall,
-                                                  sbatch.p, kSmall, ss.p, su.p, kSmall, sv.p,
-                                                  kSmall, &lw, prm, (int)n_small));
-    DevBuf work((int64_t)lw + 1);
-    sinfo.upload(std::vector<int>(n_small, 0));
-    GQ_SOLVER(cusolverDnDgesvdjBatched(h, CUSOLVER_EIG_MODE_VECTOR, kSmall, kSmall, sbatch.p,
-                                       kSmall, ss.p, su.p, kSmall, sv.p, kSmall, work.p, lw,
-                                       sinfo.p, prm, (int)n_small));
+    small_svd_kernel<<<(unsigned)n_small, 256, 0, s>>>(sbatch.p, su.p, sv.p, ss.p);
+    GQ_CUDA(cudaGetLastError());
     // X = Ux S Vx^T with X = Theta^T: Theta's left vectors are Vx (sv),
     // its right vectors Ux (su)
     for (Group *g : groups)
@@ -775,11 +879,9 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   prof_end(kProfSvdEig, 0.0, 0.0);
   // ---- values to the host ---------------------------------------------------
   std::vector<double> hs_small(n_small * kSmall), hs_j(js_total), hw(w_total);
-  std::vector<int> hinfo_s(n_small), hinfo_j(groups.size(), 0), hinfo_e(n_gram, 0);
+  std::vector<int> hinfo_j(groups.size(), 0), hinfo_e(n_gram, 0);
   if (n_small > 0) {
     GQ_CUDA(cudaMemcpyAsync(hs_small.data(), ss.p, sizeof(double) * hs_small.size(),
-                            cudaMemcpyDeviceToHost, s));
-    GQ_CUDA(cudaMemcpyAsync(hinfo_s.data(), sinfo.p, sizeof(int) * n_small,
                             cudaMemcpyDeviceToHost, s));
   }
   if (js_total > 0) {
@@ -794,8 +896,6 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
                             cudaMemcpyDeviceToHost, s));
   }
   sync();
-  for (int v : hinfo_s)
-    if (v != 0) fail(kSolverError, "batched gesvdj did not converge, info=" + std::to_string(v));
   for (int v : hinfo_j)
     if (v != 0) fail(kSolverError, "gesvdj did not converge, info=" + std::to_string(v));
   for (int v : hinfo_e)

@@ -195,7 +195,10 @@ def test_split_form_every_sweep_matches_fp64(lib, name):
 def test_split_form_batched_chains_match_fp64_single_runs(lib):
     """Batched XXZ chains in the split form (FP32-split products with FP64
     Lanczos and FP64-accurate Rayleigh energies), run concurrently, against
-    the same chains run one at a time in the plain FP64 form."""
+    the same chains run one at a time in the plain FP64 form, 6 sweeps each:
+    within 1e-9 relative for every chain whose last FP64 sweep moved its
+    energy by less than 1e-8 relative, 5e-8 for a chain still converging
+    (see test_split_form_every_sweep_matches_fp64)."""
     from mps2_gb300.vmps import DMRGState, LanczosParams, SweepParams, run_batch
     cases = [(16, 0.6, 64), (20, 1.2, 64), (24, 0.9, 128), (18, 1.45, 32), (22, 0.75, 96),
              (16, 1.1, 48)]
@@ -207,21 +210,25 @@ def test_split_form_batched_chains_match_fp64_single_runs(lib):
         DirectStateInitMps(mps, H.neel_shuffled_labels(L, L), qn0)
         return mps, mpo
 
-    fp64 = []
+    sweeps = 6
+    fp64, settled = [], []
     for L, delta, D in cases:
         mps, mpo = chain(L, delta)
         st = DMRGState(mps.tens, mpo)
         st.init_envs("fp64")
-        fp64.append(st.sweep(SweepParams(4, D, D, 0.0, lp, precision="fp64"))[0])
+        e = [st.sweep(SweepParams(1, D, D, 0.0, lp, precision="fp64"))[0] for _ in range(sweeps)]
+        fp64.append(e[-1])
+        settled.append(abs(e[-1] - e[-2]) <= CONVERGED * abs(e[-1]))
     states, params = [], []
     for L, delta, D in cases:
         mps, mpo = chain(L, delta)
         states.append(DMRGState(mps.tens, mpo))
-        params.append(SweepParams(4, D, D, 0.0, lp, precision="tf32x3", rayleigh="fp64tc"))
+        params.append(SweepParams(sweeps, D, D, 0.0, lp, precision="tf32x3", rayleigh="fp64tc"))
     split = run_batch(states, params, init_envs=True, nthreads=3)
     dev = [abs(s - e) / abs(e) for s, e in zip(split, fp64)]
-    print("batched split vs FP64 single |dE/E|:", dev)
-    assert max(dev) <= SPLIT_E_RTOL, dev
+    print("batched split vs FP64 single |dE/E|:", dev, "settled:", settled)
+    for d, ok in zip(dev, settled):
+        assert d <= (SPLIT_E_RTOL if ok else SPLIT_TRANSIENT_RTOL), (dev, settled)
 
 
 def _scale_leg(t, leg, s):
