@@ -122,6 +122,14 @@ int gq_synchronize(void);
 int gq_tensor_create(int rank, int nq, const int *dirs, const int *nsecs, const int *qns,
                      const int64_t *dims, const int *div, int64_t nblocks,
                      const int *coords, const double *data, gq_tensor **out);
+/* The same with each block's elements at its own address: blocks[nblocks]
+ * (not in the reference; spares the caller gathering the blocks into one
+ * buffer).  Both copy through pinned staging and return with the copy
+ * complete. */
+int gq_tensor_create_blocks(int rank, int nq, const int *dirs, const int *nsecs,
+                            const int *qns, const int64_t *dims, const int *div,
+                            int64_t nblocks, const int *coords,
+                            const double *const *blocks, gq_tensor **out);
 /* Sizes needed to export: rank, nq, total sector count over legs, blocks,
  * elements. */
 int gq_tensor_describe(const gq_tensor *t, int *rank, int *nq, int64_t *nsec_total,

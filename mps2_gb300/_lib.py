@@ -92,6 +92,8 @@ EXPORTS = {
     "gq_profile_enable": (_I, [_I]),
     "gq_profile_read": (_I, [_I, _I64P, _DP, _DP, _DP]),
     "gq_get_stream": (_I, [_PP]),
+    "gq_tensor_create_blocks": (_I, [_I, _I, _IP, _IP, _IP, _I64P, _IP, _I64, _IP,
+                                     C.POINTER(_DP), _PP]),
     "gq_host_sync_count": (_I, [_I64P]),
 }
 
@@ -163,14 +165,17 @@ class DeviceTensor:
         dv, pdv = _iarr(list(div))
         coords = t.sorted_block_coords()
         cd, pcd = _iarr([c for cc in coords for c in cc] or [0])
-        if coords:
-            data = np.ascontiguousarray(np.concatenate([t.blocks[c].ravel() for c in coords]),
-                                        dtype=np.float64)
-        else:
-            data = np.zeros(1)
         out = C.c_void_p()
-        check(lib.gq_tensor_create(rank, nq, pdirs, pnsecs, pqns, pdims, pdv, len(coords), pcd,
-                                   data.ctypes.data_as(_DP), C.byref(out)))
+        if not coords:
+            data = np.zeros(1)
+            check(lib.gq_tensor_create(rank, nq, pdirs, pnsecs, pqns, pdims, pdv, 0, pcd,
+                                       data.ctypes.data_as(_DP), C.byref(out)))
+            return cls(out.value)
+        # each block from its own buffer: no host-side gather into one array
+        blocks = [np.ascontiguousarray(t.blocks[c], dtype=np.float64) for c in coords]
+        ptrs = (_DP * len(blocks))(*[b.ctypes.data_as(_DP) for b in blocks])
+        check(lib.gq_tensor_create_blocks(rank, nq, pdirs, pnsecs, pqns, pdims, pdv, len(coords),
+                                          pcd, ptrs, C.byref(out)))
         return cls(out.value)
 
     def describe(self):
@@ -191,7 +196,7 @@ class DeviceTensor:
         dims = np.zeros(max(ns, 1), np.int64)
         div = np.zeros(nq, np.int32)
         coords = np.zeros(max(nb * rank, 1), np.int32)
-        data = np.zeros(max(ne, 1), np.float64)
+        data = np.empty(max(ne, 1), np.float64)
         check(load().gq_tensor_export(
             self.h, dirs.ctypes.data_as(_IP), nsecs.ctypes.data_as(_IP), qns.ctypes.data_as(_IP),
             dims.ctypes.data_as(_I64P), div.ctypes.data_as(_IP), coords.ctypes.data_as(_IP),
@@ -211,6 +216,7 @@ class DeviceTensor:
             c = tuple(int(v) for v in coords[b * rank:(b + 1) * rank])
             shape = t.block_shape(c)
             n = int(np.prod(shape))
-            t.blocks[c] = data[off:off + n].reshape(shape).copy() if with_data else np.zeros(shape)
+            # views of the one exported buffer (no second host copy)
+            t.blocks[c] = data[off:off + n].reshape(shape) if with_data else np.zeros(shape)
             off += n
         return t

@@ -75,7 +75,7 @@ def build(verbose: bool = False, extra=()) -> str:
     if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= newest):
         libdir = os.path.join(cuda_home(), "lib64")
         cmd = [_nvcc(), "-shared", "-o", LIB] + objs + ARCH + [
-            "-L", libdir, "-lcusolver", "-lcublas", "-lcudart",
+            "-L", libdir, "-lcusolver", "-lcublas", "-lcudart", "-lpthread",
             "-Xlinker", f"-rpath,{libdir}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

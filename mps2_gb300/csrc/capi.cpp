@@ -88,11 +88,11 @@ int gq_synchronize(void) {
   return guarded([&] { gq::sync(); });
 }
 
-int gq_tensor_create(int rank, int nq, const int *dirs, const int *nsecs, const int *qns,
-                     const int64_t *dims, const int *div, int64_t nblocks, const int *coords,
-                     const double *data, gq_tensor **out) {
-  return guarded([&] {
-    GQ_CHECK(out, "null output handle");
+namespace {
+// Structure of a tensor from the C arrays of gq_tensor_create, validated.
+gq::TensorPtr structure_from_c(int rank, int nq, const int *dirs, const int *nsecs,
+                               const int *qns, const int64_t *dims, const int *div,
+                               int64_t nblocks, const int *coords) {
     GQ_CHECK(rank >= 1 && rank <= gq::kMaxRank, "rank out of range");
     GQ_CHECK(nq >= 1 && nq <= gq::kMaxQ, "nq out of range");
     GQ_CHECK(dirs && nsecs && qns && dims && div, "null structure array");
@@ -122,15 +122,45 @@ int gq_tensor_create(int rank, int nq, const int *dirs, const int *nsecs, const 
     auto t = gq::make_structure(nq, idx, d, blocks);
     for (int64_t b = 0; b < t->nblocks(); ++b)
       GQ_CHECK(t->block_div(t->block_coords(b)) == d, "block breaks the tensor's divergence");
+    return t;
+}
+}  // namespace
+
+int gq_tensor_create(int rank, int nq, const int *dirs, const int *nsecs, const int *qns,
+                     const int64_t *dims, const int *div, int64_t nblocks, const int *coords,
+                     const double *data, gq_tensor **out) {
+  return guarded([&] {
+    GQ_CHECK(out, "null output handle");
+    auto t = structure_from_c(rank, nq, dirs, nsecs, qns, dims, div, nblocks, coords);
     t->allocate();
     if (data) {
-      if (t->size() > 0)
-        GQ_CUDA(cudaMemcpyAsync(t->data.p, data, sizeof(double) * t->size(),
-                                cudaMemcpyHostToDevice, gq::stream()));
-      gq::sync();  // the caller may free `data` on return
+      // complete on return: the caller may free `data`
+      gq::copy_h2d(t->data.p, data, sizeof(double) * t->size());
     } else {
       t->zero();
     }
+    *out = wrap(t);
+  });
+}
+
+int gq_tensor_create_blocks(int rank, int nq, const int *dirs, const int *nsecs,
+                            const int *qns, const int64_t *dims, const int *div,
+                            int64_t nblocks, const int *coords, const double *const *blocks,
+                            gq_tensor **out) {
+  return guarded([&] {
+    GQ_CHECK(out, "null output handle");
+    GQ_CHECK(blocks || nblocks == 0, "null block pointer array");
+    auto t = structure_from_c(rank, nq, dirs, nsecs, qns, dims, div, nblocks, coords);
+    t->allocate();
+    std::vector<const void *> src((size_t)nblocks);
+    std::vector<size_t> sz((size_t)nblocks);
+    for (int64_t b = 0; b < nblocks; ++b) {
+      GQ_CHECK(blocks[b], "null block data");
+      src[b] = blocks[b];
+      sz[b] = sizeof(double) * (size_t)t->block_size(b);
+    }
+    // complete on return: the caller may free the blocks
+    gq::copy_h2d_gather(t->data.p, src.data(), sz.data(), (size_t)nblocks);
     *out = wrap(t);
   });
 }
@@ -169,11 +199,7 @@ int gq_tensor_export(const gq_tensor *h, int *dirs, int *nsecs, int *qns, int64_
     if (div)
       for (int k = 0; k < t.nq; ++k) div[k] = t.div.v[k];
     if (coords) std::copy(t.coords.begin(), t.coords.end(), coords);
-    if (data && t.size() > 0) {
-      GQ_CUDA(cudaMemcpyAsync(data, t.data.p, sizeof(double) * t.size(), cudaMemcpyDeviceToHost,
-                              gq::stream()));
-      gq::sync();
-    }
+    if (data && t.size() > 0) gq::copy_d2h(data, t.data.p, sizeof(double) * t.size());
   });
 }
 

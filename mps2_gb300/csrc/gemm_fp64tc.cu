@@ -74,6 +74,34 @@ __device__ __forceinline__ float round_f32(float x) {
   if (!(fabsf(x) < big)) return x;
   return x >= 0.0f ? (x + big) - big : (x - big) + big;
 }
+// x 2^e as a double, rounded to nearest even, from integer operations only
+// (the same value as ldexp((double)x, e) whenever the result is a normal
+// double; the caller takes that expression otherwise -- flagged by ok).
+__device__ __forceinline__ double scaled_i64_to_f64(long long x, int e, bool &ok) {
+  ok = true;
+  if (x == 0) return 0.0;
+  const unsigned long long sign = x < 0 ? 1ull : 0ull;
+  const unsigned long long mag = sign ? 0ull - (unsigned long long)x : (unsigned long long)x;
+  const int lz = __clzll((long long)mag);
+  const unsigned long long norm = mag << lz;  // leading one at bit 63
+  unsigned long long sig = norm >> 11;        // 53 bits
+  const unsigned long long rem = norm & 0x7ffull;
+  int biased = 63 - lz + e + 1023;
+  if (rem > 0x400ull || (rem == 0x400ull && (sig & 1ull))) {
+    sig += 1ull;
+    if (sig == (1ull << 53)) {
+      sig >>= 1;
+      biased += 1;
+    }
+  }
+  if (biased <= 0 || biased >= 2047) {
+    ok = false;
+    return 0.0;
+  }
+  return __longlong_as_double((long long)((sign << 63) | ((unsigned long long)biased << 52) |
+                                          (sig & ((1ull << 52) - 1ull))));
+}
+
 // An integer-valued float (|x| < 2^63) as int64, from its bits: the
 // significand shifted by the exponent.
 __device__ __forceinline__ long long integral_f32_to_i64(float x) {
@@ -506,8 +534,11 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
         const int cl = cbase + j;
         const int ec = sm.colexp[cl];
         double x = 0.0;
-        if (nchunks > 0 && oz::valid_exp(er) && oz::valid_exp(ec))
-          x = ldexp((double)run[j], er + ec - 44);
+        if (nchunks > 0 && oz::valid_exp(er) && oz::valid_exp(ec)) {
+          bool ok;
+          x = oz::scaled_i64_to_f64(run[j], er + ec - 44, ok);
+          if (!ok) x = ldexp((double)run[j], er + ec - 44);
+        }
         tile[lrow * oz::BN + cl] = x;
       }
     }

@@ -26,6 +26,10 @@ struct Lane {
   void *cublas = nullptr;          // cublasHandle_t, created lazily
   char *staging = nullptr;         // pinned ring for work-list uploads
   size_t staging_head = 0;
+  // Two pinned buffers for large copies of caller memory (copy_h2d/d2h),
+  // with the events of their last DMA; allocated on first use.
+  char *xfer[2] = {nullptr, nullptr};
+  cudaEvent_t xfer_done[2] = {nullptr, nullptr};
   // Auxiliary streams for independent library calls inside one operation
   // (the block SVD's eigensolves of different sizes run side by side),
   // forked from and joined back to `stream` with events; created on first
@@ -73,6 +77,14 @@ void lane_destroy(Lane *l);
 void lane_bind(Lane *l);   // bind to this thread (nullptr: the main lane)
 bool on_main_lane();
 void sync();                // wait for this thread's lane stream (counted)
+// Copies of caller (pageable) memory to and from the device on the lane's
+// stream, pipelined through the lane's pinned buffers: the host copy of one
+// chunk (split over host threads) overlaps the DMA of the other.  Both
+// return with the copy complete.
+void copy_h2d(void *dst, const void *src, size_t bytes);
+// The same for the concatenation of nseg host segments (srcs[i], sizes[i]).
+void copy_h2d_gather(void *dst, const void *const *srcs, const size_t *sizes, size_t nseg);
+void copy_d2h(void *dst, const void *src, size_t bytes);
 int64_t host_sync_count();  // waits by sync() since load, all threads
 
 // Kernel profiling with CUDA events on the library stream (off by default).

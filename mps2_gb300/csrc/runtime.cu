@@ -6,7 +6,10 @@
 #include <chrono>
 #include <cstring>
 #include <map>
+#include <algorithm>
 #include <mutex>
+#include <thread>
+#include <vector>
 
 namespace gq {
 
@@ -102,6 +105,10 @@ void lane_destroy(Lane *l) {
   cudaStreamSynchronize(l->stream);
   cudaFreeHost(l->host_scalars);
   if (l->staging) cudaFreeHost(l->staging);
+  for (int k = 0; k < 2; ++k) {
+    if (l->xfer[k]) cudaFreeHost(l->xfer[k]);
+    if (l->xfer_done[k]) cudaEventDestroy(l->xfer_done[k]);
+  }
   if (l->fork_event) {
     for (int i = 0; i < Lane::kAux; ++i) {
       cudaStreamSynchronize(l->aux_stream[i]);
@@ -156,6 +163,117 @@ std::atomic<int64_t> g_host_syncs{0};
 }  // namespace
 
 int64_t host_sync_count() { return g_host_syncs.load(); }
+
+namespace {
+constexpr size_t kXferBytes = size_t(64) << 20;   // per pinned buffer
+constexpr size_t kXferDirect = size_t(1) << 20;   // below: one plain copy
+constexpr int kXferThreads = 8;
+
+// Bytes [lo, hi) of the concatenation of the segments (starts pre[i], the
+// last entry the total) into dst, split over up to kXferThreads host
+// threads for large ranges.
+void host_gather(char *dst, const char *const *segs, const std::vector<size_t> &pre, size_t lo,
+                 size_t hi) {
+  auto part_copy = [&](size_t b, size_t e) {
+    size_t i = (size_t)(std::upper_bound(pre.begin(), pre.end(), b) - pre.begin()) - 1;
+    while (b < e) {
+      const size_t end = std::min(e, pre[i + 1]);
+      if (end > b) std::memcpy(dst + (b - lo), segs[i] + (b - pre[i]), end - b);
+      b = end;
+      ++i;
+    }
+  };
+  const size_t bytes = hi - lo;
+  const int nt = bytes >= (size_t(8) << 20) ? kXferThreads : 1;
+  if (nt == 1) {
+    part_copy(lo, hi);
+    return;
+  }
+  const size_t part = (bytes + nt - 1) / nt;
+  std::vector<std::thread> th;
+  th.reserve(nt - 1);
+  for (int t = 1; t < nt; ++t) {
+    const size_t b = lo + std::min(bytes, t * part), e = lo + std::min(bytes, (t + 1) * part);
+    if (b < e) th.emplace_back(part_copy, b, e);
+  }
+  part_copy(lo, lo + std::min(bytes, part));
+  for (auto &x : th) x.join();
+}
+
+void host_copy(char *dst, const char *src, size_t bytes) {
+  const char *seg[1] = {src};
+  host_gather(dst, seg, {0, bytes}, 0, bytes);
+}
+
+void xfer_setup(Lane &l) {
+  for (int k = 0; k < 2; ++k) {
+    if (!l.xfer[k]) GQ_CUDA(cudaMallocHost((void **)&l.xfer[k], kXferBytes));
+    if (!l.xfer_done[k])
+      GQ_CUDA(cudaEventCreateWithFlags(&l.xfer_done[k], cudaEventDisableTiming));
+  }
+}
+}  // namespace
+
+void copy_h2d_gather(void *dst, const void *const *srcs, const size_t *sizes, size_t nseg) {
+  Lane &l = lane();
+  std::vector<size_t> pre(nseg + 1, 0);
+  for (size_t i = 0; i < nseg; ++i) pre[i + 1] = pre[i] + sizes[i];
+  const size_t bytes = pre[nseg];
+  if (bytes == 0) return;
+  const char *const *segs = reinterpret_cast<const char *const *>(srcs);
+  char *d = static_cast<char *>(dst);
+  if (nseg == 1 && bytes <= kXferDirect) {
+    GQ_CUDA(cudaMemcpyAsync(dst, srcs[0], bytes, cudaMemcpyHostToDevice, l.stream));
+    sync();
+    return;
+  }
+  xfer_setup(l);
+  size_t off = 0;
+  for (int c = 0; off < bytes; ++c) {
+    const int k = c & 1;
+    const size_t b = std::min(kXferBytes, bytes - off);
+    GQ_CUDA(cudaEventSynchronize(l.xfer_done[k]));  // its previous DMA is done
+    host_gather(l.xfer[k], segs, pre, off, off + b);
+    GQ_CUDA(cudaMemcpyAsync(d + off, l.xfer[k], b, cudaMemcpyHostToDevice, l.stream));
+    GQ_CUDA(cudaEventRecord(l.xfer_done[k], l.stream));
+    off += b;
+  }
+  sync();
+}
+
+void copy_h2d(void *dst, const void *src, size_t bytes) {
+  const void *seg[1] = {src};
+  copy_h2d_gather(dst, seg, &bytes, 1);
+}
+
+void copy_d2h(void *dst, const void *src, size_t bytes) {
+  Lane &l = lane();
+  if (bytes == 0) return;
+  if (bytes <= kXferDirect) {
+    GQ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, l.stream));
+    sync();
+    return;
+  }
+  xfer_setup(l);
+  const char *s = static_cast<const char *>(src);
+  char *d = static_cast<char *>(dst);
+  const int nchunks = (int)((bytes + kXferBytes - 1) / kXferBytes);
+  auto chunk = [&](int c) { return std::min(kXferBytes, bytes - (size_t)c * kXferBytes); };
+  auto issue = [&](int c) {
+    const int k = c & 1;
+    GQ_CUDA(cudaMemcpyAsync(l.xfer[k], s + (size_t)c * kXferBytes, chunk(c),
+                            cudaMemcpyDeviceToHost, l.stream));
+    GQ_CUDA(cudaEventRecord(l.xfer_done[k], l.stream));
+  };
+  issue(0);
+  for (int c = 0; c < nchunks; ++c) {
+    // the buffer of chunk c + 1 held chunk c - 1, whose host copy is done
+    if (c + 1 < nchunks) issue(c + 1);
+    GQ_CUDA(cudaEventSynchronize(l.xfer_done[c & 1]));
+    host_copy(d + (size_t)c * kXferBytes, l.xfer[c & 1], chunk(c));
+  }
+  sync();
+}
 
 void sync() {
   g_host_syncs.fetch_add(1, std::memory_order_relaxed);

@@ -62,6 +62,9 @@ constexpr int kSmall = 32;
 // rows run on 4-CTA clusters, larger ones on 16-CTA clusters.
 constexpr double kPcTol = 1e-15;
 constexpr int64_t kPcSmallRows = 512;
+// Eigensolve buckets holding one matrix of at least this size use the
+// divide-and-conquer solver instead of the batched one.
+constexpr int64_t kSyevdMinRows = 128;
 
 enum Route { kSmallJacobi = 0, kJacobi = 1, kGramLeft = 2, kGramRight = 3 };
 
@@ -120,13 +123,15 @@ cublasHandle_t blas() {
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
-struct GatherItem { int64_t src_off, dst_off; int rows, cols, ld; };
+// Elements [e0, e1) of one block per CTA (blocks are cut into chunks of at
+// most kCopyChunk elements, so one large block does not serialise a launch).
+constexpr int64_t kCopyChunk = 16384;
+struct GatherItem { int64_t src_off, dst_off, e0, e1; int rows, cols, ld; };
 
 __global__ void gather_kernel(const GatherItem *__restrict__ items, const double *__restrict__ src,
                               double *__restrict__ dst) {
   const GatherItem it = items[blockIdx.x];
-  const int64_t n = (int64_t)it.rows * it.cols;
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+  for (int64_t e = it.e0 + threadIdx.x; e < it.e1; e += blockDim.x) {
     const int64_t i = e / it.cols, j = e % it.cols;
     dst[it.dst_off + i * it.ld + j] = src[it.src_off + e];
   }
@@ -333,7 +338,7 @@ __global__ void sign_fix_kernel(const SignItem *__restrict__ items, double *__re
 // Output blocks.  mode 0: U block (rows x k, row-major), element (i, j) =
 // L[r0 + i, j]; mode 1: Vt block (k x rows), element (j, i) = R[r0 + i, j];
 // L and R are the group's col-major factors (ld = group m or n).
-struct ScatterItem { int64_t dst_off, src_off; int rows, k, ld, mode; };
+struct ScatterItem { int64_t dst_off, src_off, e0, e1; int rows, k, ld, mode; };
 
 __global__ void scatter_kernel(const ScatterItem *__restrict__ items, const double *__restrict__ L,
                                const double *__restrict__ R, double *__restrict__ U,
@@ -341,8 +346,7 @@ __global__ void scatter_kernel(const ScatterItem *__restrict__ items, const doub
   const ScatterItem it = items[blockIdx.x];
   const double *src = it.mode == 0 ? L : R;
   double *dst = it.mode == 0 ? U : Vt;
-  const int64_t n = (int64_t)it.rows * it.k;
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+  for (int64_t e = it.e0 + threadIdx.x; e < it.e1; e += blockDim.x) {
     int i, j;
     if (it.mode == 0) { i = (int)(e / it.k); j = (int)(e % it.k); }
     else { j = (int)(e / it.rows); i = (int)(e % it.rows); }
@@ -574,8 +578,11 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       Group &g = gmap[br.q];
       const int64_t ri = std::lower_bound(g.rows.begin(), g.rows.end(), br.rc) - g.rows.begin();
       const int64_t ci = std::lower_bound(g.cols.begin(), g.cols.end(), br.cc) - g.cols.begin();
-      items.push_back({t.offs[br.b], g.mat_off + g.roff[ri] * g.n + g.coff[ci], (int)g.rsz[ri],
-                       (int)g.csz[ci], (int)g.n});
+      const int64_t n = g.rsz[ri] * g.csz[ci];
+      for (int64_t e0 = 0; e0 < n; e0 += kCopyChunk)
+        items.push_back({t.offs[br.b], g.mat_off + g.roff[ri] * g.n + g.coff[ci], e0,
+                         std::min(n, e0 + kCopyChunk), (int)g.rsz[ri], (int)g.csz[ci],
+                         (int)g.n});
     }
     launch_items(gather_kernel, items, t.data.p, mats.p);
   }
@@ -659,8 +666,10 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   // Either matrix goes into a slot padded to a bucket size with -1 on the
   // extra diagonal, so the padding's eigenpairs sort below the real ones and
   // stay in the padded coordinates; one batched eigensolve per bucket.
-  // Bucket sizes: 32 (cuSOLVER's batched Jacobi range), 64, one bucket for
-  // 65..256 padded to the largest of them, multiples of 64 above.
+  // Bucket sizes: multiples of 32 up to 256, of 64 above (the padding of a
+  // matrix to its bucket costs up to (bucket / size)^3 in work: measured
+  // over a D=4000 run, one bucket for all of 65..256 padded to the largest
+  // of them took 7.5 of 24 s of eigensolves).
   std::vector<Group *> gram;
   int64_t gbuf_total = 0, q_total = 0, t_total = 0;
   for (Group *g : groups)
@@ -742,19 +751,13 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   }
   prof_end(kProfSvdReduce, 0.0, 0.0);
   auto bucket_of = [](int64_t real) -> int64_t {
-    if (real <= 32) return 32;
-    if (real <= 64) return 64;
+    if (real <= 256) return (real + 31) / 32 * 32;
     return (real + 63) / 64 * 64;
   };
   std::map<int64_t, std::vector<Group *>> buckets;
-  int64_t mid_dim = 0;
-  for (Group *g : gram) {
-    g->dim = (g->pc && g->r == 0) ? 0 : bucket_of(g->pc ? g->r : g->gn);
-    if (g->dim > 64 && g->dim <= 256) mid_dim = std::max(mid_dim, g->dim);
-  }
+  for (Group *g : gram) g->dim = (g->pc && g->r == 0) ? 0 : bucket_of(g->pc ? g->r : g->gn);
   for (Group *g : gram) {
     if (g->dim == 0) continue;  // a zero matrix: nothing to solve
-    if (g->dim > 64 && g->dim <= 256) g->dim = mid_dim;
     buckets[g->dim].push_back(g);
   }
   int64_t ev_total = 0, w_total = 0, n_gram = 0;
@@ -824,13 +827,23 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       params.v.push_back(x);
     }
     const std::vector<cusolverDnParams_t> &sp = params.v;
+    // A bucket holding one large matrix goes to the divide-and-conquer
+    // solver: measured over a D=4000 run, the batched call took 10-20 ms for
+    // one matrix of 320-960 rows.
+    auto single = [](const Solve &v) { return v.nb == 1 && v.bs >= kSyevdMinRows; };
     std::vector<size_t> dws(nslot, 0), hws(nslot, 0);
     for (const Solve &v : solves) {
       size_t d1 = 0, h1 = 0;
-      GQ_SOLVER(cusolverDnXsyevBatched_bufferSize(
-          handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
-          CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off, CUDA_R_64F,
-          &d1, &h1, v.nb));
+      if (single(v))
+        GQ_SOLVER(cusolverDnXsyevd_bufferSize(
+            handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
+            CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off,
+            CUDA_R_64F, &d1, &h1));
+      else
+        GQ_SOLVER(cusolverDnXsyevBatched_bufferSize(
+            handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
+            CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off,
+            CUDA_R_64F, &d1, &h1, v.nb));
       dws[v.slot] = std::max(dws[v.slot], d1);
       hws[v.slot] = std::max(hws[v.slot], h1);
     }
@@ -848,12 +861,20 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       // released -- on an error too, since the workspaces are freed in
       // stream order on the lane's stream
       AuxJoin joined(ln, nslot - 1);
-      for (const Solve &v : solves)
-        GQ_SOLVER(cusolverDnXsyevBatched(
-            handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, v.bs,
-            CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F, w.p + v.first->w_off,
-            CUDA_R_64F, dwork[v.slot].p, dws[v.slot], hwork[v.slot].data(), hws[v.slot],
-            einfo.p + v.io, v.nb));
+      for (const Solve &v : solves) {
+        if (single(v))
+          GQ_SOLVER(cusolverDnXsyevd(
+              handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+              v.bs, CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F,
+              w.p + v.first->w_off, CUDA_R_64F, dwork[v.slot].p, dws[v.slot],
+              hwork[v.slot].data(), hws[v.slot], einfo.p + v.io));
+        else
+          GQ_SOLVER(cusolverDnXsyevBatched(
+              handle_of(v.slot), sp[v.slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+              v.bs, CUDA_R_64F, ev.p + v.first->ev_off, v.bs, CUDA_R_64F,
+              w.p + v.first->w_off, CUDA_R_64F, dwork[v.slot].p, dws[v.slot],
+              hwork[v.slot].data(), hws[v.slot], einfo.p + v.io, v.nb));
+      }
     }
   }
   // eigenvectors of the reduced groups: U = Q Z (gn x r), Z the slot's
@@ -1183,15 +1204,21 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
         auto c = g->rows[ri];
         c.push_back(g->sector);
         const int64_t ob = out.u->find(c.data());
-        items.push_back({out.u->offs[ob], g->L_off + g->roff[ri], (int)g->rsz[ri], (int)g->keep,
-                         (int)g->m, 0});
+        const int64_t n = g->rsz[ri] * g->keep;
+        for (int64_t e0 = 0; e0 < n; e0 += kCopyChunk)
+          items.push_back({out.u->offs[ob], g->L_off + g->roff[ri], e0,
+                           std::min(n, e0 + kCopyChunk), (int)g->rsz[ri], (int)g->keep,
+                           (int)g->m, 0});
       }
       for (size_t ci = 0; ci < g->cols.size(); ++ci) {
         std::vector<int> c{g->sector};
         c.insert(c.end(), g->cols[ci].begin(), g->cols[ci].end());
         const int64_t ob = out.vt->find(c.data());
-        items.push_back({out.vt->offs[ob], g->R_off + g->coff[ci], (int)g->csz[ci], (int)g->keep,
-                         (int)g->n, 1});
+        const int64_t n = g->csz[ci] * g->keep;
+        for (int64_t e0 = 0; e0 < n; e0 += kCopyChunk)
+          items.push_back({out.vt->offs[ob], g->R_off + g->coff[ci], e0,
+                           std::min(n, e0 + kCopyChunk), (int)g->csz[ci], (int)g->keep,
+                           (int)g->n, 1});
       }
     }
     DevArray<ScatterItem> d;
