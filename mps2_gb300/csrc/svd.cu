@@ -428,34 +428,50 @@ void dense_contract_tc(const double *A, int64_t a0, int64_t a1, int axa, const d
 // factor of the complete Householder QR of `vecs` -- the unit vectors
 // e_r .. e_{r+k-1} carried through its r reflectors (geqrf, then ormqr on
 // the shifted identity; LAPACK's reflector conventions, as the oracle's
-// numpy QR, on the vectors with signed zeros made +0.0).  O(dim r (r + k)) work, exactly orthonormal whatever the
-// overlap of the unit vectors with `vecs`.  The status words of the two
-// calls go to info_dev[0..1] (checked later by the caller).
-void null_completion(const double *vecs, int64_t dim, int64_t r, int64_t k, double *out,
-                     int *info_dev) {
-  if (k == 0) return;
+// numpy QR, on the vectors with signed zeros made +0.0).  O(dim r (r + k))
+// work, exactly orthonormal whatever the overlap of the unit vectors with
+// `vecs`.  In two steps: prepare (on the lane's stream: the shifted
+// identity, the QR input, the workspace) and factor (geqrf + ormqr with the
+// given handle, so that the completions of one SVD can run side by side on
+// the lane's auxiliary streams).  The status words of the two calls go to
+// info[0..1] (checked later by the caller).
+struct Completion {
+  DevBuf q;              // the r input vectors (dim x r)
+  DevBuf a, tau, work;   // QR input and factors, workspace
+  int64_t dim = 0, r = 0, k = 0;
+  int lw = 0;
+  double *out = nullptr;
+  int *info = nullptr;
+};
+
+void completion_prepare(Completion &c) {
+  if (c.k == 0) return;
   auto s = stream();
-  const unsigned grid = (unsigned)std::min<int64_t>((dim * k + 255) / 256, 4096);
-  shifted_identity_kernel<<<grid, 256, 0, s>>>(out, (int)dim, (int)k, (int)r);
+  const unsigned grid = (unsigned)std::min<int64_t>((c.dim * c.k + 255) / 256, 4096);
+  shifted_identity_kernel<<<grid, 256, 0, s>>>(c.out, (int)c.dim, (int)c.k, (int)c.r);
   GQ_CUDA(cudaGetLastError());
-  if (r == 0) return;
-  prof_begin(kProfSvdOrtho);
+  if (c.r == 0) return;
   auto sh = solver();
-  const int d = (int)dim, kk = (int)k, rr = (int)r;
-  DevBuf a(dim * r), tau(r);
-  plus_zero_copy_kernel<<<(unsigned)std::min<int64_t>((dim * r + 255) / 256, 4096), 256, 0, s>>>(
-      vecs, a.p, dim * r);
+  const int d = (int)c.dim, kk = (int)c.k, rr = (int)c.r;
+  c.a.alloc(c.dim * c.r);
+  c.tau.alloc(c.r);
+  plus_zero_copy_kernel<<<(unsigned)std::min<int64_t>((c.dim * c.r + 255) / 256, 4096), 256, 0,
+                          s>>>(c.q.p, c.a.p, c.dim * c.r);
   GQ_CUDA(cudaGetLastError());
   int lw1 = 0, lw2 = 0;
-  GQ_SOLVER(cusolverDnDgeqrf_bufferSize(sh, d, rr, a.p, d, &lw1));
-  GQ_SOLVER(cusolverDnDormqr_bufferSize(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, d, kk, rr, a.p, d,
-                                        tau.p, out, d, &lw2));
-  const int lw = std::max(lw1, lw2);
-  DevBuf work((int64_t)lw + 1);
-  GQ_SOLVER(cusolverDnDgeqrf(sh, d, rr, a.p, d, tau.p, work.p, lw, info_dev));
-  GQ_SOLVER(cusolverDnDormqr(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, d, kk, rr, a.p, d, tau.p, out, d,
-                             work.p, lw, info_dev + 1));
-  prof_end(kProfSvdOrtho, 0.0, 0.0);
+  GQ_SOLVER(cusolverDnDgeqrf_bufferSize(sh, d, rr, c.a.p, d, &lw1));
+  GQ_SOLVER(cusolverDnDormqr_bufferSize(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, d, kk, rr, c.a.p, d,
+                                        c.tau.p, c.out, d, &lw2));
+  c.lw = std::max(lw1, lw2);
+  c.work.alloc((int64_t)c.lw + 1);
+}
+
+void completion_factor(Completion &c, cusolverDnHandle_t sh) {
+  if (c.k == 0 || c.r == 0) return;
+  const int d = (int)c.dim, kk = (int)c.k, rr = (int)c.r;
+  GQ_SOLVER(cusolverDnDgeqrf(sh, d, rr, c.a.p, d, c.tau.p, c.work.p, c.lw, c.info));
+  GQ_SOLVER(cusolverDnDormqr(sh, CUBLAS_SIDE_LEFT, CUBLAS_OP_N, d, kk, rr, c.a.p, d, c.tau.p,
+                             c.out, d, c.work.p, c.lw, c.info + 1));
 }
 
 struct Group {
@@ -1137,13 +1153,17 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     cinfo.upload(std::vector<int>(2 * ncomp + 2, 0));
   }
   int64_t cslot = 0;
+  std::vector<Completion> comps;
+  comps.reserve(2 * groups.size());
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     Group *g = groups[gi];
     const int64_t kz = g->keep - g->keep_nz;
     if (kz == 0) continue;
     auto completion = [&](bool left, double *dst) {
       const int64_t dim = left ? g->m : g->n;
-      DevBuf q(std::max<int64_t>(dim * g->nnz, 1));
+      comps.emplace_back();
+      Completion &c = comps.back();
+      c.q.alloc(std::max<int64_t>(dim * g->nnz, 1));
       std::vector<ColItem> items;
       const bool gram = g->route == kGramLeft || g->route == kGramRight;
       for (int64_t j = 0; j < g->nnz; ++j)
@@ -1154,13 +1174,41 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       const double *src = gram ? (g->pc ? ubuf.p : ev.p)
                                : g->route == kSmallJacobi ? (left ? sv.p : su.p)
                                                           : (left ? jl.p : jr.p);
-      launch_items(col_copy_kernel, items, src, q.p);
-      null_completion(q.p, dim, g->nnz, kz, dst, cinfo.p + cslot);
+      launch_items(col_copy_kernel, items, src, c.q.p);
+      c.dim = dim;
+      c.r = g->nnz;
+      c.k = kz;
+      c.out = dst;
+      c.info = cinfo.p + cslot;
+      completion_prepare(c);
       cslot += 2;
     };
     if (eig_is_canonical(g)) continue;  // zero columns came with the eigenvectors
     if (scale_side != 1) completion(true, Lb.p + g->L_off + g->keep_nz * g->m);
     if (scale_side != 2) completion(false, Rb.p + g->R_off + g->keep_nz * g->n);
+  }
+  // the factorisations, dealt round-robin over the lane's stream and its
+  // auxiliary streams (each with its own handle), joined back before the
+  // buffers above are released
+  {
+    int nfac = 0;
+    for (auto &c : comps) nfac += (c.k > 0 && c.r > 0) ? 1 : 0;
+    if (nfac > 0) {
+      prof_begin(kProfSvdOrtho);
+      const int nslot = std::min(nfac, 1 + Lane::kAux);
+      Lane &ln = lane();
+      fork_aux(ln, nslot - 1);
+      {
+        AuxJoin joined(ln, nslot - 1);
+        int i = 0;
+        for (auto &c : comps) {
+          if (c.k == 0 || c.r == 0) continue;
+          const int slot = i++ % nslot;
+          completion_factor(c, slot == 0 ? solver() : aux_solver(slot - 1));
+        }
+      }
+      prof_end(kProfSvdOrtho, 0.0, 0.0);
+    }
   }
 
   prof_end(kProfSvdFactors, 0.0, 0.0);
