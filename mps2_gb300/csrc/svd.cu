@@ -64,7 +64,7 @@ constexpr double kPcTol = 1e-15;
 constexpr int64_t kPcSmallRows = 512;
 // Eigensolve buckets holding one matrix of at least this size use the
 // divide-and-conquer solver instead of the batched one.
-constexpr int64_t kSyevdMinRows = 128;
+constexpr int64_t kSyevdMinRows = 320;
 
 enum Route { kSmallJacobi = 0, kJacobi = 1, kGramLeft = 2, kGramRight = 3 };
 
@@ -168,15 +168,15 @@ __device__ __forceinline__ double warp_sum_all(double v) {
   return v;
 }
 
-// Column at position j of round `round` of the round-robin pairing of 32
-// columns (position 0 fixed, the other 31 rotating).
-__device__ __forceinline__ int rr_column(int j, int round) {
-  return j == 0 ? 0 : (j - 1 + round) % (kSmall - 1) + 1;
+// Column at position j of round `round` of the round-robin pairing of nc
+// columns (nc even; position 0 fixed, the other nc - 1 rotating).
+__device__ __forceinline__ int rr_column(int j, int round, int nc) {
+  return j == 0 ? 0 : (j - 1 + round) % (nc - 1) + 1;
 }
 
 __global__ void __launch_bounds__(256)
-    small_svd_kernel(const double *__restrict__ X, double *__restrict__ U,
-                     double *__restrict__ V, double *__restrict__ S) {
+    small_svd_kernel(const double *__restrict__ X, const int *__restrict__ ncols,
+                     double *__restrict__ U, double *__restrict__ V, double *__restrict__ S) {
   __shared__ double w[kSmall][kSmall + 1];  // w[column][row]
   __shared__ double v[kSmall][kSmall + 1];
   __shared__ double sig[kSmall];
@@ -205,11 +205,13 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   const double neg = negligible;
+  // only the slot's own columns take part (the padding columns are zero)
+  const int nc = min(kSmall, max(2, (ncols[blockIdx.x] + 1) & ~1));
   for (int sweep = 0; sweep < kSmallSweeps; ++sweep) {
     int mine = 0;
-    for (int round = 0; round < kSmall - 1; ++round) {
-      for (int pi = warp; pi < kSmall / 2; pi += nwarps) {
-        const int p = rr_column(pi, round), q = rr_column(kSmall - 1 - pi, round);
+    for (int round = 0; round < nc - 1; ++round) {
+      for (int pi = warp; pi < nc / 2; pi += nwarps) {
+        const int p = rr_column(pi, round, nc), q = rr_column(nc - 1 - pi, round, nc);
         const double a = w[p][lane], b = w[q][lane];
         const double alpha = warp_sum_all(a * a), beta = warp_sum_all(b * b);
         const double gamma = warp_sum_all(a * b);
@@ -422,6 +424,47 @@ void dense_contract_tc(const double *A, int64_t a0, int64_t a1, int axa, const d
                           stream()));
 }
 
+// Independent FP64 GEMMs gathered into one grouped batched cuBLAS call
+// (each product its own group of one): the per-group products of the block
+// SVD are many and mostly small, and one call replaces a library launch
+// sequence per group.
+struct GemmBatch {
+  std::vector<cublasOperation_t> ta, tb;
+  std::vector<int> m, n, k, lda, ldb, ldc, size;
+  std::vector<double> alpha, beta;
+  std::vector<const double *> A, B;
+  std::vector<double *> C;
+  void add(cublasOperation_t a_op, cublasOperation_t b_op, int m_, int n_, int k_,
+           const double *A_, int lda_, const double *B_, int ldb_, double *C_, int ldc_) {
+    ta.push_back(a_op);
+    tb.push_back(b_op);
+    m.push_back(m_);
+    n.push_back(n_);
+    k.push_back(k_);
+    A.push_back(A_);
+    lda.push_back(lda_);
+    B.push_back(B_);
+    ldb.push_back(ldb_);
+    C.push_back(C_);
+    ldc.push_back(ldc_);
+    alpha.push_back(1.0);
+    beta.push_back(0.0);
+    size.push_back(1);
+  }
+  void run(cublasHandle_t h) {
+    if (A.empty()) return;
+    DevArray<const double *> dA, dB;
+    DevArray<double *> dC;
+    dA.upload(A);
+    dB.upload(B);
+    dC.upload(C);
+    GQ_BLAS(cublasDgemmGroupedBatched(h, ta.data(), tb.data(), m.data(), n.data(), k.data(),
+                                      alpha.data(), dA.p, lda.data(), dB.p, ldb.data(),
+                                      beta.data(), dC.p, ldc.data(), (int)A.size(),
+                                      size.data()));
+  }
+};
+
 // Canonical completion: k orthonormal columns orthogonal to the r
 // orthonormal columns of `vecs` (dim x r, col-major, ld dim), written to
 // out (dim x k, col-major, ld dim): columns r .. r+k-1 of the orthogonal
@@ -625,7 +668,12 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
       if (g->route == kSmallJacobi)
         items.push_back({g->mat_off, g->small_idx * slot, (int)g->n, (int)g->m});
     launch_items(pad_small_kernel, items, mats.p, sbatch.p);
-    small_svd_kernel<<<(unsigned)n_small, 256, 0, s>>>(sbatch.p, su.p, sv.p, ss.p);
+    std::vector<int> cols(n_small, 0);
+    for (Group *g : groups)
+      if (g->route == kSmallJacobi) cols[g->small_idx] = (int)g->m;  // columns of X = Theta^T
+    DevArray<int> dcols;
+    dcols.upload(cols);
+    small_svd_kernel<<<(unsigned)n_small, 256, 0, s>>>(sbatch.p, dcols.p, su.p, sv.p, ss.p);
     GQ_CUDA(cudaGetLastError());
     // X = Ux S Vx^T with X = Theta^T: Theta's left vectors are Vx (sv),
     // its right vectors Ux (su)
@@ -712,7 +760,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   DevBuf gbuf(gbuf_total), lbuf(q_total), qbuf(q_total), tbuf(t_total), cbuf(t_total);
   prof_begin(kProfSvdGram);
   {
-    const double one = 1.0, zero = 0.0;
+    GemmBatch gb;
     for (Group *g : gram) {
       const int m = (int)g->m, n = (int)g->n, gd = (int)g->gn;
       const double *X = mats.p + g->mat_off;  // col-major n x m
@@ -723,11 +771,12 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
         const int ax = g->eig_m ? 1 : 0;
         dense_contract_tc(X, m, n, ax, X, m, n, ax, G);
       } else if (g->eig_m) {  // Theta Theta^T = X^T X (m x m)
-        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, X, n, X, n, &zero, G, m));
+        gb.add(CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, X, n, X, n, G, m);
       } else {  // Theta^T Theta = X X^T (n x n)
-        GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_T, n, n, m, &one, X, n, X, n, &zero, G, n));
+        gb.add(CUBLAS_OP_N, CUBLAS_OP_T, n, n, m, X, n, X, n, G, n);
       }
     }
+    gb.run(bh);
   }
   prof_end(kProfSvdGram, 0.0, 0.0);
   prof_begin(kProfSvdReduce);
@@ -903,15 +952,15 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
     }
   DevBuf ubuf(u_total);
   {
-    const double one = 1.0, zero = 0.0;
+    GemmBatch gb;
     for (Group *g : gram) {
       if (!g->pc || g->r == 0) continue;
       const int gd = (int)g->gn, r = g->r, bs = (int)g->dim;
       // Q row-major gn x rcap is col-major rcap x gn: op(A) = A^T
-      GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, gd, r, r, &one, qbuf.p + g->q_off, g->rcap,
-                          ev.p + g->ev_off + (int64_t)(bs - r) * bs, bs, &zero,
-                          ubuf.p + g->u_off, gd));
+      gb.add(CUBLAS_OP_T, CUBLAS_OP_N, gd, r, r, qbuf.p + g->q_off, g->rcap,
+             ev.p + g->ev_off + (int64_t)(bs - r) * bs, bs, ubuf.p + g->u_off, gd);
     }
+    gb.run(bh);
   }
   prof_end(kProfSvdEig, 0.0, 0.0);
   // ---- values to the host ---------------------------------------------------
@@ -1102,7 +1151,7 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
   // projections for the Gram routes: R = X L (canonical left) or L = X^T R
   // (canonical right)
   {
-    const double one = 1.0, zero = 0.0;
+    GemmBatch gb;
     for (Group *g : groups) {
       if (g->keep_nz == 0 || (g->route != kGramLeft && g->route != kGramRight)) continue;
       const int m = (int)g->m, n = (int)g->n, k = (int)g->keep_nz;
@@ -1114,21 +1163,20 @@ SvdOut svd_truncate(const Tensor &t_in, int ldims, const QN &ldiv, double trunc_
         if (tc)
           dense_contract_tc(R, k, n, 1, X, m, n, 1, L);
         else
-          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_T, CUBLAS_OP_N, m, k, n, &one, X, n, R, n, &zero, L,
-                              m));
+          gb.add(CUBLAS_OP_T, CUBLAS_OP_N, m, k, n, X, n, R, n, L, m);
       };
       auto right_from_left = [&] {  // R = X L (n x k): Rrow = Lrow . Theta
         if (tc)
           dense_contract_tc(L, k, m, 1, X, m, n, 0, R);
         else
-          GQ_BLAS(cublasDgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, &one, X, n, L, m, &zero, R,
-                              n));
+          gb.add(CUBLAS_OP_N, CUBLAS_OP_N, n, k, m, X, n, L, m, R, n);
       };
       if (g->route == kGramLeft)
         right_from_left();
       else
         left_from_right();
     }
+    gb.run(bh);
   }
   // sign convention on the kept nonzero columns (by the left factor)
   {
