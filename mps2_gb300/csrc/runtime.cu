@@ -131,10 +131,14 @@ cudaStream_t stream() { return lane().stream; }
 // run.  A cudaMemcpyAsync from pageable memory synchronises the stream
 // first, which would drain the GPU at every plan built between two kernels
 // (the SVD's projections and the environment growth build several); the
-// lists are staged through a pinned ring per lane instead.  Regions of the
-// ring are reused only after it wraps, behind a stream synchronisation.
+// lists are staged through a pinned ring per lane instead.  Every wait on
+// the lane's stream (sync()) empties the ring, since every copy from it has
+// then run; between two waits the ring wraps behind a stream
+// synchronisation only when it is full -- which, with a Lanczos loop queued
+// as one graph, would hold the host until the whole loop has run, so the
+// ring is sized to hold an update's work lists.
 namespace {
-constexpr size_t kStagingBytes = size_t(16) << 20;
+constexpr size_t kStagingBytes = size_t(64) << 20;
 }
 
 void upload_async(void *dst, const void *src, size_t bytes) {
@@ -277,12 +281,15 @@ void copy_d2h(void *dst, const void *src, size_t bytes) {
 
 void sync() {
   g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+  Lane &l = lane();
   if (!prof_on()) {
-    GQ_CUDA(cudaStreamSynchronize(stream()));
+    GQ_CUDA(cudaStreamSynchronize(l.stream));
+    l.staging_head = 0;  // every staged copy has run
     return;
   }
   const auto t0 = std::chrono::steady_clock::now();
-  GQ_CUDA(cudaStreamSynchronize(stream()));
+  GQ_CUDA(cudaStreamSynchronize(l.stream));
+  l.staging_head = 0;
   prof_host(kProfHostSync,
             std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
 }
