@@ -166,9 +166,9 @@ int gq_contract(const gq_tensor *a, const gq_tensor *b, int naxes, const int *ax
  * looks the arrays up and loads this entry point's kernels on its device
  * (CUDA loads modules lazily, and that load may allocate); without gq_init,
  * the first call on a device does it, so make that first call before the
- * no-allocation phase and before any stream capture.  Each call returns
- * after its GPU work has finished.  Calls share the arrays: calls that
- * overlap on the GPU race. */
+ * no-allocation phase.  Each call returns after its GPU work has finished
+ * (it waits on the library stream, so it cannot be captured into a CUDA
+ * graph).  Calls share the arrays: calls that overlap on the GPU race. */
 int gq_contract_noalloc(const gq_tensor *a, const gq_tensor *b, int naxes, const int *axes_a,
                         const int *axes_b, gq_tensor *out);
 

@@ -115,7 +115,10 @@ __device__ __forceinline__ long long integral_f32_to_i64(float x) {
 }
 constexpr int kThreads = 320;          // 8 merge warps, producer, MMA issuer
 constexpr int kMergeThreads = 256;
-constexpr int kMaxK = 1 << 16;          // k of one tile, summed over its pairs
+// k of one tile, summed over its pairs: per k the running sum grows by at
+// most sum_g (g+1) 2^14 2^(-8g) 2^30 < 1.008 * 2^44 (digit products below
+// 2^14 on the 2^-30 grid), so 2^18 of k stay below 2^62.02 < 2^63.
+constexpr int kMaxK = 1 << 18;
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000ll;
 constexpr int kNoExp = -(1 << 30);            // column outside the tile

@@ -113,6 +113,23 @@ def test_fp64tc_integer_operands_are_exact(lib):
     assert rel_err(got, ref) == 0.0
 
 
+def test_fp64tc_long_k_beyond_two_to_the_sixteen(lib):
+    """A thin block pair with k = 70000 > 2^16 (as the J1-J2 cylinder's
+    environment contractions have): runs on the FP64-accurate kernel, within
+    the tolerance of the others."""
+    from mps2_gb300.vmps import Contract
+    rng = np.random.default_rng(12)
+    r = Index([((0,), 9)], OUT)
+    k = Index([((0,), 70000)], OUT)
+    c = Index([((0,), 7)], OUT)
+    a = GQTensor([r, k], (0,), {(0, 0): rng.standard_normal((9, 70000))})
+    b = GQTensor([k.inverse(), c], (0,), {(0, 0): rng.standard_normal((70000, 7))})
+    ref = oracle.contract(to_oracle(a), to_oracle(b), [1], [0])
+    got, n = oz_launches(lambda: Contract(a, b, ([1], [0]), precision="fp64tc"))
+    assert n > 0, "the tensor-core kernel did not run"
+    assert rel_err(got, ref) <= TOL
+
+
 @pytest.mark.parametrize("where", ["cent", "lend", "rend"])
 def test_fp64tc_matvec_matches_oracle(lib, where):
     from mps2_gb300.vmps import eff_ham_mul_state
