@@ -43,6 +43,7 @@
 
 #include <unordered_map>
 
+#include "exact_convert.cuh"
 #include "gq_runtime.hpp"
 
 namespace gq {
@@ -60,59 +61,9 @@ constexpr int kBStage = kSlices * kBTile;     // 42 KB
 constexpr int kStageBytes = kAStage + kBStage;
 constexpr int kChunkSteps = 8;                // 256 k between read-outs
 
-// The merge turns FP32 accumulator values into int64 running sums.  The
-// hardware float-to-int64 conversion issues on the FP64 pipe, which on this
-// part runs ~2 operations per clock per SM (61k conversions per 256-k chunk
-// of a 128 x 96 tile would outlast the chunk's MMAs), so both steps below
-// use the FP32 and integer pipes only.
-//
-// x rounded to the nearest integer, ties to even: adding and removing 2^23
-// with the sign of x rounds a float of magnitude below 2^23 (FP32 adds round
-// to nearest even); larger floats are integers already.
-__device__ __forceinline__ float round_f32(float x) {
-  const float big = 8388608.0f;  // 2^23
-  if (!(fabsf(x) < big)) return x;
-  return x >= 0.0f ? (x + big) - big : (x - big) + big;
-}
-// x 2^e as a double, rounded to nearest even, from integer operations only
-// (the same value as ldexp((double)x, e) whenever the result is a normal
-// double; the caller takes that expression otherwise -- flagged by ok).
-__device__ __forceinline__ double scaled_i64_to_f64(long long x, int e, bool &ok) {
-  ok = true;
-  if (x == 0) return 0.0;
-  const unsigned long long sign = x < 0 ? 1ull : 0ull;
-  const unsigned long long mag = sign ? 0ull - (unsigned long long)x : (unsigned long long)x;
-  const int lz = __clzll((long long)mag);
-  const unsigned long long norm = mag << lz;  // leading one at bit 63
-  unsigned long long sig = norm >> 11;        // 53 bits
-  const unsigned long long rem = norm & 0x7ffull;
-  int biased = 63 - lz + e + 1023;
-  if (rem > 0x400ull || (rem == 0x400ull && (sig & 1ull))) {
-    sig += 1ull;
-    if (sig == (1ull << 53)) {
-      sig >>= 1;
-      biased += 1;
-    }
-  }
-  if (biased <= 0 || biased >= 2047) {
-    ok = false;
-    return 0.0;
-  }
-  return __longlong_as_double((long long)((sign << 63) | ((unsigned long long)biased << 52) |
-                                          (sig & ((1ull << 52) - 1ull))));
-}
-
-// An integer-valued float (|x| < 2^63) as int64, from its bits: the
-// significand shifted by the exponent.
-__device__ __forceinline__ long long integral_f32_to_i64(float x) {
-  const uint32_t u = __float_as_uint(x);
-  const int e = (int)((u >> 23) & 0xffu);
-  if (e < 127) return 0;  // |x| < 1: zero (x is an integer)
-  const uint64_t m = (uint64_t)((u & 0x7fffffu) | 0x800000u);
-  const int sh = e - 150;  // x = m 2^sh, sh >= -23
-  const uint64_t mag = sh >= 0 ? (m << (sh < 39 ? sh : 39)) : (m >> -sh);
-  return (u >> 31) ? -(long long)mag : (long long)mag;
-}
+// The merge turns the FP32 accumulator values into int64 running sums and
+// the write-back the sums into doubles, both with the integer and FP32
+// pipes only (exact_convert.cuh).
 constexpr int kThreads = 320;          // 8 merge warps, producer, MMA issuer
 constexpr int kMergeThreads = 256;
 // k of one tile, summed over its pairs: per k the running sum grows by at
@@ -512,12 +463,12 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
           if (a < oz::kAcc - 1) {
 #pragma unroll
             for (int j = 0; j < 16; ++j)  // orders 0..3: x * 2^30 is an exact integer
-              run[cb * 16 + j] += oz::integral_f32_to_i64(__uint_as_float(f[j]) * two30);
+              run[cb * 16 + j] += xconv::integral_f32_to_i64(__uint_as_float(f[j]) * two30);
           } else {
 #pragma unroll
             for (int j = 0; j < 16; ++j)  // orders 4..6: rounded to the nearest integer
               run[cb * 16 + j] +=
-                  oz::integral_f32_to_i64(oz::round_f32(__uint_as_float(f[j]) * two30));
+                  xconv::integral_f32_to_i64(xconv::round_f32(__uint_as_float(f[j]) * two30));
           }
         }
       }
@@ -539,7 +490,7 @@ __global__ void __launch_bounds__(oz::kThreads, 1)
         double x = 0.0;
         if (nchunks > 0 && oz::valid_exp(er) && oz::valid_exp(ec)) {
           bool ok;
-          x = oz::scaled_i64_to_f64(run[j], er + ec - 44, ok);
+          x = xconv::scaled_i64_to_f64(run[j], er + ec - 44, ok);
           if (!ok) x = ldexp((double)run[j], er + ec - 44);
         }
         tile[lrow * oz::BN + cl] = x;

@@ -21,6 +21,7 @@
 // records an error code, drains, frees its TMEM and exits.
 #include <cstdint>
 
+#include "exact_convert.cuh"
 #include "gq_runtime.hpp"
 
 namespace gq {
@@ -58,23 +59,6 @@ struct PackTask { int block, rt, kt; };
 // integer and FP32 pipes).  hi = round-to-nearest(x) to 11 significant
 // bits; lo = the next 11 significant bits of (fl32(x) - hi).  Magnitudes
 // below FP32's normal range are flushed to zero.
-// A float's exact value as a double, from integer operations (the
-// conversion instruction issues on the FP64 pipe, ~2 per clock per SM on
-// this part: three FP64 operations per element made the write-back of a
-// short-k tile outlast its MMAs).
-__device__ __forceinline__ double f32_bits_to_f64(uint32_t u) {
-  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-  if (e == 0) {
-    if (m == 0) return __longlong_as_double((long long)sign);
-    const int sh = __clz((int)m) - 8;  // leading one of a subnormal to bit 23
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(897 - sh) << 52) |
-                                            ((unsigned long long)((m << sh) & 0x7fffffu) << 29)));
-  }
-  const unsigned long long ex = e == 255u ? 2047ull : (unsigned long long)(e + 896u);
-  return __longlong_as_double((long long)(sign | (ex << 52) | ((unsigned long long)m << 29)));
-}
-
 __device__ __forceinline__ void split_tf32(double x, uint32_t &hi, uint32_t &lo) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const uint32_t sign = (uint32_t)(b >> 63) << 31;
@@ -433,7 +417,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1)
             for (int j = 0; j < 32; ++j) {
               const int col = t.col0 + cb * 32 + j;
               if (col < t.n)
-                crow[col] = f32_bits_to_f64(hv[j]) + f32_bits_to_f64(lv[j]);
+                // hi and lo as doubles from their bits (exact_convert.cuh), one FP64 add
+                crow[col] = xconv::f32_bits_to_f64(hv[j]) + xconv::f32_bits_to_f64(lv[j]);
             }
           }
         }
