@@ -85,7 +85,20 @@ double measure_ee(const std::vector<double> &s) {
 }
 }  // namespace
 
-UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
+Dmrg::~Dmrg() {
+  for (auto &e : env_ev)
+    if (e) cudaEventDestroy(e);
+}
+
+void Dmrg::resolve_env_time() {
+  if (env_pending && env_ev[1]) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, env_ev[0], env_ev[1]) == cudaSuccess) *env_pending = ms * 1e-3;
+  }
+  env_pending = nullptr;
+}
+
+UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target, bool overlap) {
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
   const int Nn = N();
@@ -125,6 +138,7 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
   lp.rayleigh = prm.lanczos.rayleigh;
   auto res = lanczos(h, *space, lp, prec);
   sync();
+  resolve_env_time();  // the previous update's growth is done by now
   st.lanczos_seconds = seconds_since(tl);
   st.iters = res.iters;
   st.e0 = res.energy;
@@ -145,6 +159,11 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
   mps[c.rs] = sv.vt;  // 'r': S.Vt
 
   const auto te = clk::now();
+  if (overlap) {
+    for (auto &e : env_ev)
+      if (!e) GQ_CUDA(cudaEventCreate(&e));
+    GQ_CUDA(cudaEventRecord(env_ev[0], stream()));
+  }
   double f1 = 0, f2 = 0, f3 = 0;
   if (dir == 'r') {
     if (target != Nn - 2) {
@@ -173,10 +192,14 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
       }
     }
   }
-  sync();
-  st.env_seconds = seconds_since(te);
+  if (overlap) {
+    GQ_CUDA(cudaEventRecord(env_ev[1], stream()));  // env_seconds: filled in later
+  } else {
+    sync();
+    st.env_seconds = seconds_since(te);
+    check_device_errors();
+  }
   st.env_flops = f1 + f2 + f3;
-  check_device_errors();
   st.update_seconds = seconds_since(t0);
   if (prm.verbose) {
     // the reference's stream state: fixed, precision 16 for E0, 2 after the
@@ -193,16 +216,26 @@ UpdateStatsC Dmrg::update(const SweepParamsC &prm, char dir, int target) {
 double Dmrg::sweep(const SweepParamsC &prm, std::vector<UpdateStatsC> *stats) {
   const int Nn = N();
   double e0 = 0.0;
-  for (int i = 0; i < Nn - 1; ++i) {
-    auto st = update(prm, 'r', i);
+  // the pending environment time points into `stats`: no reallocation
+  // during the sweep, and no pointer left behind on any exit
+  struct PendingReset {
+    Dmrg &d;
+    ~PendingReset() { d.env_pending = nullptr; }
+  } reset{*this};
+  if (stats) stats->reserve(stats->size() + 2 * (size_t)std::max(Nn - 1, 0));
+  auto one = [&](char dir, int i) {
+    auto st = update(prm, dir, i, true);
     e0 = st.e0;
-    if (stats) stats->push_back(st);
-  }
-  for (int i = Nn - 1; i > 0; --i) {
-    auto st = update(prm, 'l', i);
-    e0 = st.e0;
-    if (stats) stats->push_back(st);
-  }
+    if (stats) {
+      stats->push_back(st);
+      env_pending = &stats->back().env_seconds;
+    }
+  };
+  for (int i = 0; i < Nn - 1; ++i) one('r', i);
+  for (int i = Nn - 1; i > 0; --i) one('l', i);
+  sync();
+  resolve_env_time();
+  check_device_errors();  // the tensor-core error word, once per sweep
   return e0;
 }
 

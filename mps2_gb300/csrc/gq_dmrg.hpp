@@ -33,10 +33,22 @@ struct UpdateStatsC {
 struct Dmrg {
   std::vector<TensorPtr> mps, mpo;
   std::map<std::pair<char, int>, TensorPtr> envs;
+  // Inside a sweep an update does not wait for its environment growth: the
+  // next update's host work (contraction plans, graph build) runs while the
+  // growth's kernels do.  The growth's device time is taken with two events
+  // and written to *env_pending once a later wait has seen them.
+  cudaEvent_t env_ev[2] = {nullptr, nullptr};
+  double *env_pending = nullptr;
+  Dmrg() = default;
+  Dmrg(const Dmrg &) = delete;
+  Dmrg &operator=(const Dmrg &) = delete;
+  ~Dmrg();
   int N() const { return (int)mps.size(); }
   void init_envs(Precision prec);
-  UpdateStatsC update(const SweepParamsC &prm, char dir, int target);
+  // overlap: return without waiting for the environment growth (sweeps)
+  UpdateStatsC update(const SweepParamsC &prm, char dir, int target, bool overlap = false);
   double sweep(const SweepParamsC &prm, std::vector<UpdateStatsC> *stats);
+  void resolve_env_time();  // after a wait on the stream
 };
 
 }  // namespace gq
