@@ -22,14 +22,17 @@ and Rayleigh energies, FP64 Lanczos recurrence and SVD).
   and right environments -- the drop-in call's work.
 * ``roofline``, ``kernels``, ``gpu_launches``: from one more split sweep run
   under the library's kernel profiler (CUDA events around every kernel
-  family on the library stream; the Lanczos matvec then runs launch by
-  launch instead of as a replayed CUDA graph): the kernel family with the
-  most device time, its algorithmic flops (2*m*n*k over the QN-allowed
-  block products) or bytes / its event time, against the measured peak.
+  family on the library stream; the Lanczos iteration then runs host-driven,
+  one iteration at a time, instead of as a CUDA-graph while loop): the
+  kernel family with the most device time, its algorithmic flops (2*m*n*k
+  over the QN-allowed block products) or bytes / its event time, against
+  the measured peak; with the host time spent planning contractions and
+  waiting for the device.
 * ``cpu_baseline``: the FP64 CPU restatement (numpy + the host BLAS, all
-  host threads) on real two-site updates of the same state at bonds spread
-  evenly over the chain; a sweep is estimated as 2(L-1) times their mean
-  update time.  Its energy at the centre bond is compared with the GPU's.
+  host threads) on three real two-site updates of the same state (near
+  both ends and at the centre); a sweep is estimated as 2(L-1) times their
+  mean update time.  Its energy at the centre bond is compared with the
+  GPU's.
 * ``--impl reference``: the same CPU restatement on the same kind of updates
   (block structures at eight evenly spaced bonds recorded from a GPU run of
   this workload, ``--record-structure``; random data; Lanczos capped at the
