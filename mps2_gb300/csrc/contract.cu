@@ -552,10 +552,12 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
   //  * The form's own tensor-core kernel takes a block when at least 2%
   //    (3xTF32) or 3% (FP64-accurate) of its padded work is useful: those
   //    rates are a few hundred and ~35 times this part's FP64 rate.
-  //  * Otherwise, by default, a block goes to the FP64-accurate kernel when
-  //    its padded work there costs less time than the FP64 kernel's padded
-  //    tiles: thin blocks (a few rows or columns, long k) waste most of
-  //    either tile and the FP64 pipe of this part is ~20x slower.  In the
+  //  * Otherwise (with the default threshold or an autotuner candidate below
+  //    1; the candidate above 1 keeps everything else on FP64 tiles) a block
+  //    goes to the FP64-accurate kernel when its padded work there costs
+  //    less time than the FP64 kernel's padded tiles: thin blocks (a few
+  //    rows or columns, long k) waste most of either tile and the FP64 pipe
+  //    of this part is ~20x slower.  In the
   //    split form too: there the thin blocks keep FP64 accuracy (moved to
   //    3xTF32 they shift its Lanczos convergence enough to leave the
   //    per-sweep energy parity of 1e-9).
@@ -597,7 +599,7 @@ std::shared_ptr<ContractPlan> build_plan(const Tensor &a, const Tensor &b,
       const bool oz_ok = ksum <= oz_max_k();
       if (useful >= frac * padded && (prec == kTF32x3 || oz_ok))
         kind = prec == kTF32x3 ? kKindTf32 : kKindOz;
-      else if (tc_frac < 0.0 && oz_ok && padded_oz < 20.0 * padded_fp64)
+      else if (tc_frac < 1.0 && oz_ok && padded_oz < 20.0 * padded_fp64)
         kind = kKindOz;
       if (kind == kKindTf32) plan->padded_flops += padded;
       if (kind == kKindOz) plan->padded_flops += padded_oz;
