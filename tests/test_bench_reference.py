@@ -73,3 +73,7 @@ def test_reference_update_on_recorded_structure(tmp_path, capsys):
     assert line["impl"] == "reference" and line["unit"] == "s/sweep"
     assert line["value"] == pytest.approx(2 * (L - 1) * line["ms_per_step"] * 1e-3)
     assert line["cpu_baseline"]["kind"] == "port"
+    assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "s/sweep", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["higher_is_better"] is False and line["steps"] == 2 and line["warmup"] == 1
